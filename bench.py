@@ -1,0 +1,346 @@
+"""Benchmark of the Fourier intersection-volume hot path on GB300.
+
+Workload (default): the 256-object volume matrix -- 128 icosphere-4 (5,120
+triangles, affine-deformed) + 128 boxes, random rotations, centres U[0,8]^3,
+k-grid L=64 x Lebedev-1202 (N_k = 76,928).  One step = one cold volume matrix
+from device-resident geometry: DoF transform + form factors (5.05e10
+triangle x k evaluations) + contraction V = Re(J^H D J).
+
+    python bench.py [--gpus N --steps K --warmup W] [--impl reference] [--precision fp32|bf16x3]
+
+`value`  : triangle x k evaluations per second over the whole job (inputs
+           resident in HBM; L2 flushed before every timed step).
+`e2e`    : the same metric through the C ABI's host-buffer entry point
+           pi_volume_matrix_host (host geometry in, host V out).
+Multi-GPU: weak scaling -- every rank evaluates its own seeded 256-object
+matrix; no collective on the data path.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "tri×k evals/s; vol-matrix/s BF16-TC vs FP32 at 1e-4 rel err; p50/p99 ms"
+UNIT = "tri×k evals/s"
+SFU_OPS_PER_EVAL = 9      # 3 complex exponentials (6) + 3 reciprocals, reference algorithm count
+FP32_FLOPS_PER_EVAL = 40  # reference algorithm count (FMA = 2)
+SFU_PER_SM_PER_CLK = 16   # nominal MUFU results per SM per clock
+FP32_FLOPS_PER_SM_PER_CLK = 256
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=10)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    p.add_argument("--precision", default="auto", choices=["auto", "fp32", "bf16x3"])
+    p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--no-cpu", action="store_true")
+    p.add_argument("--cpu-seconds", type=float, default=12.0)
+    return p.parse_args()
+
+
+def dist_setup(n):
+    rank, world, local = int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+    return rank, world, local
+
+
+def load_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            return json.load(fh), "measured"
+    except Exception:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0, "sm_max_mhz": 2070.0}, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                                          "-i", str(self.gpu), "-lms", "200"], stdout=self.fh, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            self.fh.close()
+
+    def summary(self):
+        out = {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        if not self.path or not os.path.exists(self.path):
+            return out
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        os.unlink(self.path)
+        if sm:
+            out.update(sm_mhz=statistics.median(sm), sm_max_mhz=max(mx), reasons=sorted(reasons), samples=len(sm))
+        return out
+
+
+def cpu_baseline_matrix256(objs, kg, seconds: float, sample_offset: int = 0):
+    """FP64 oracle (the reference algorithm restated; OpenMP over all host
+    threads) on a strided subset of k-nodes of the same workload."""
+    from oracle import oracle as orc
+    oobjs = [orc.Obj(o.geom.type, o.geom.elems, o.dof_type, o.dofs) for o in objs]
+    n_tri = sum(len(o.elems) for o in oobjs)
+    Q = kg.num_nodes
+    # calibrate on a tiny sample, then size the stride for ~`seconds`
+    stride = 4096
+    t0 = time.perf_counter()
+    orc.form_factor_matrix(oobjs, kg.dirs, kg.kmag, stride=stride)
+    dt = max(time.perf_counter() - t0, 1e-3)
+    per_node = dt / len(range(0, Q, stride))
+    n_nodes = max(1, int(seconds / per_node))
+    stride = max(1, Q // n_nodes)
+    sel = np.arange(sample_offset % stride, Q, stride)
+    t0 = time.perf_counter()
+    J = orc.form_factor_matrix(oobjs, kg.dirs[sel], kg.kmag[sel])
+    orc.contract(J, kg.w[sel])
+    dt = time.perf_counter() - t0
+    evals = n_tri * len(sel)
+    return {"value": evals / dt, "unit": UNIT, "cores": orc.max_threads(), "kind": "port",
+            "sample": f"{len(sel)} of {Q} k-nodes (every {stride}th) x {n_tri} triangles, form factors + contraction, FP64",
+            "seconds": dt}
+
+
+def run_reference(args):
+    rank, world, local = dist_setup(args.gpus)
+    if rank != 0:
+        return
+    from pointint_gb300 import configs
+    from oracle import oracle as orc
+    kg, objs, meta = configs.matrix256(seed=0)
+    per_step = max(2.0, min(10.0, 150.0 / max(1, args.steps + args.warmup)))
+    for w in range(args.warmup):
+        cpu_baseline_matrix256(objs, kg, per_step / 4, sample_offset=w)
+    vals, secs = [], []
+    for s in range(args.steps):
+        r = cpu_baseline_matrix256(objs, kg, per_step, sample_offset=s + 1)
+        vals.append(r["value"])
+        secs.append(r["seconds"])
+    v = float(statistics.median(vals))
+    n_tri = meta["n_triangles"]
+    evals_step = n_tri * kg.num_nodes
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * evals_step / v, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
+            "config": {"workload": meta["workload"], "n_k": kg.num_nodes, "seed": 0,
+                       "note": "reference CPU path (FP64 oracle port, OpenMP) on a strided k-node sample per step; "
+                               "ms_per_step extrapolated to the full matrix"},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": orc.max_threads(), "kind": "port",
+                             "sample": r["sample"]},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def run_gb300(args):
+    import torch
+    rank, world, local = dist_setup(args.gpus)
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    from pointint_gb300 import configs, core, _lib
+    peaks, peak_src = load_peaks()
+    kg, objs, meta = configs.matrix256(seed=rank)
+    n_obj = len(objs)
+    n_tri = meta["n_triangles"]
+    Q = kg.num_nodes
+    evals_step = n_tri * Q
+    precision = args.precision
+    if precision == "auto":
+        precision = "fp32"
+        try:
+            probe_ws = core.contract_workspace_size(kg, n_obj, "bf16x3")
+            torch.zeros(1, device="cuda")
+            Jt = torch.zeros((n_obj, Q), dtype=torch.complex64, device="cuda")
+            core.contract(kg, Jt, "bf16x3")
+            precision = "bf16x3"
+            del Jt, probe_ws
+        except _lib.PointIntError:
+            precision = "fp32"
+    stream = torch.cuda.current_stream()
+    batch = core.ObjectBatch(objs)
+    Jw = torch.empty((n_obj, Q), dtype=torch.complex64, device="cuda")
+    V = torch.empty((n_obj, n_obj), dtype=torch.float64, device="cuda")
+    ws = core.Workspace()
+    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device="cuda")  # > 129 MB L2
+
+    def step(ev_ff=None):
+        batch.prepare()
+        if ev_ff:
+            ev_ff[0].record(stream)
+        core.form_factors(kg, batch, True, out=Jw)
+        if ev_ff:
+            ev_ff[1].record(stream)
+        core.contract(kg, Jw, precision, out=V, workspace=ws)
+
+    for _ in range(max(3, args.warmup)):
+        step()
+    torch.cuda.synchronize()
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+    torch.cuda.synchronize()
+    launches0 = _lib.launch_count()
+    total_ms, ff_ms = 0.0, 0.0
+    with ClockSampler(local) as clk:
+        for _ in range(args.steps):
+            flush.zero_()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            step((f0, f1))
+            e1.record(stream)
+            e1.synchronize()
+            total_ms += e0.elapsed_time(e1)
+            ff_ms += f0.elapsed_time(f1)
+        torch.cuda.synchronize()
+    launches = _lib.launch_count() - launches0
+    clocks = clk.summary()
+    t = torch.tensor([total_ms], dtype=torch.float64, device="cuda")
+    if world > 1:
+        import torch.distributed as dist
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        dist.barrier()
+    total_ms = float(t.item())
+    ms_per_step = total_ms / args.steps
+    value = world * evals_step * args.steps / (total_ms / 1e3)
+
+    # contraction alone: FP32 vs BF16 split (warm: resident J)
+    def time_contract(p, reps=20):
+        core.contract(kg, Jw, p, out=V, workspace=ws)
+        torch.cuda.synchronize()
+        ms = []
+        for _ in range(reps):
+            flush.zero_()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            core.contract(kg, Jw, p, out=V, workspace=ws)
+            b.record(stream)
+            b.synchronize()
+            ms.append(a.elapsed_time(b))
+        return statistics.median(ms)
+
+    contraction = {"fp32_ms": time_contract("fp32")}
+    V32 = V.clone()
+    if precision == "bf16x3":
+        contraction["bf16x3_ms"] = time_contract("bf16x3")
+        d = torch.sqrt(torch.outer(torch.diagonal(V32), torch.diagonal(V32)).abs())
+        rel = ((V - V32).abs() / torch.maximum(V32.abs(), 1e-3 * d)).max().item()
+        contraction["bf16x3_vs_fp32_max_rel"] = rel
+        contraction["speedup"] = contraction["fp32_ms"] / contraction["bf16x3_ms"]
+
+    sm_clock = clocks.get("sm_mhz") or peaks.get("sm_max_mhz", 2070.0)
+    n_sm = torch.cuda.get_device_properties(local).multi_processor_count
+    ff_avg_s = ff_ms / args.steps / 1e3
+    sfu_achieved = SFU_OPS_PER_EVAL * evals_step / ff_avg_s / 1e9
+    sfu_peak = n_sm * SFU_PER_SM_PER_CLK * float(peaks.get("sm_max_mhz", 2070.0)) * 1e6 / 1e9
+    fp32_achieved = FP32_FLOPS_PER_EVAL * evals_step / ff_avg_s / 1e12
+    fp32_peak = n_sm * FP32_FLOPS_PER_SM_PER_CLK * float(peaks.get("sm_max_mhz", 2070.0)) * 1e6 / 1e12
+    roofline = {"kernel": "ff_kernel", "bound": "sfu", "achieved": sfu_achieved, "peak": sfu_peak, "unit": "Gop/s",
+                "frac": sfu_achieved / sfu_peak, "traffic": FF_TRAFFIC_BYTES_PER_LAUNCH,
+                "kernel_ms": ff_avg_s * 1e3, "share_of_step": (ff_ms / total_ms) if world == 1 else None,
+                "algorithmic_unit": f"{SFU_OPS_PER_EVAL} SFU ops per triangle x k evaluation x {evals_step:.4e} evaluations",
+                "peak_source": f"nominal {SFU_PER_SM_PER_CLK} MUFU/clk/SM x {n_sm} SMs x {peaks.get('sm_max_mhz', 2070.0)} MHz "
+                               f"(MEASURED_PEAKS.json has no SFU/FP32 figure; {peak_src} file)",
+                "fp32": {"achieved": fp32_achieved, "peak": fp32_peak, "unit": "TFLOP/s", "frac": fp32_achieved / fp32_peak}}
+
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32", "data": "synthetic (seeded)",
+            "config": {"workload": meta["workload"], "n_k": Q, "n_objects": n_obj, "n_triangles": n_tri,
+                       "mix": meta["mix"], "seed": "rank", "contraction": precision,
+                       "l2": "flushed (256 MB write) before every timed step", "parallelism": f"replicas x{world}"},
+            "vol_matrix_per_s": world * args.steps / (total_ms / 1e3),
+            "contraction": contraction, "clocks": clocks, "gpu_launches": launches, "roofline": roofline}
+
+    if rank == 0 and not args.no_e2e:
+        line["e2e"] = e2e_host(kg, objs, precision, args.steps, evals_step, world)
+    if rank == 0 and world == 1 and not args.no_cpu:
+        try:
+            line["cpu_baseline"] = {k: v for k, v in cpu_baseline_matrix256(objs, kg, args.cpu_seconds).items()
+                                    if k != "seconds"}
+        except Exception as exc:  # the oracle must not break the GPU line
+            line["cpu_baseline"] = {"value": None, "error": str(exc)}
+    if rank == 0:
+        print(json.dumps(line))
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+FF_TRAFFIC_BYTES_PER_LAUNCH = None
+
+
+def e2e_host(kg, objs, precision, steps, evals_step, world):
+    """Same metric through pi_volume_matrix_host: host geometry + host k-grid in,
+    host V out, uploads and downloads inside the timed region."""
+    from pointint_gb300 import core
+    core.volume_matrix_host(kg, objs, precision)  # warm-up
+    n = len(objs)
+    h2d = sum(o.geom.elems.nbytes + o.dofs.nbytes for o in objs) + kg.dirs.nbytes + kg.kmag.nbytes + kg.w.nbytes
+    d2h = n * n * 8
+    reps = max(3, min(steps, 10))
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        core.volume_matrix_host(kg, objs, precision)
+    dt = (time.perf_counter() - t0) / reps
+    return {"value": world * evals_step / dt, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": d2h,
+            "ms_per_step": dt * 1e3, "entry_point": "pi_volume_matrix_host"}
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gb300(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,180 @@
+/*
+ * pointint_gb300 -- C ABI of the GB300-native Fourier intersection-volume path.
+ *
+ * Drop-in boundary for PoIntInt's Fourier path (reference paths are inside the
+ * PoIntInt project).  Every entry point returns an int status (PI_OK == 0);
+ * pi_last_error() gives the message of the last failure on the calling thread.
+ * Nothing is ever silently zeroed: the reference printed CUDA errors and
+ * returned zeros (cpp/src/compute_intersection_volume.cu:243-262, 473-486);
+ * here the caller always sees a status.
+ *
+ * Memory: entry points named *_host take host buffers and do their own
+ * uploads/downloads (the reference's calling convention).  All other entry
+ * points take caller-owned DEVICE buffers, run on the given stream and never
+ * synchronize the device implicitly.
+ *
+ * Element layouts are byte-identical to the reference's TriPacked / DiskPacked /
+ * GaussianPacked (cpp/include/geometry/types.hpp:9-37), so a C++ caller can
+ * pass geom.tris.data() / geom.disks.data() / geom.gaussians.data() as is.
+ * K-grids are passed as the three arrays of the reference's KGrid
+ * (cpp/include/quadrature/kgrid.hpp:9-13): dirs (Q x 3), kmag (Q), w (Q).
+ * Volumes carry the 1/(8 pi^3) factor; k-grid weights do not.
+ */
+#ifndef POINTINT_GB300_H
+#define POINTINT_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* cudaStream_t without pulling in the CUDA headers. */
+typedef struct CUstream_st* pi_stream;
+
+/* ---- status codes -------------------------------------------------------- */
+enum {
+  PI_OK = 0,
+  PI_ERR_INVALID_ARGUMENT = 1,
+  PI_ERR_CUDA = 2,
+  PI_ERR_UNSUPPORTED = 3,
+  PI_ERR_OUT_OF_MEMORY = 4,
+  PI_ERR_NOT_FOUND = 5,
+  PI_ERR_WORKSPACE_TOO_SMALL = 6,
+  PI_ERR_IO = 7,
+  PI_ERR_TIMEOUT = 8
+};
+
+/* Geometry types: reference GeometryType (cpp/include/geometry/types.hpp:40-44). */
+enum { PI_GEOM_TRIANGLE = 0, PI_GEOM_DISK = 1, PI_GEOM_GAUSSIAN = 2 };
+/* DoF parameterizations: AffineDoF (cpp/include/dof/affine_dof.hpp:8-14) and
+ * TriangleMeshDoF (cpp/include/dof/triangle_mesh_dof.hpp). */
+enum { PI_DOF_AFFINE = 0, PI_DOF_TRIANGLE_MESH = 1 };
+/* ComputationFlags (cpp/include/computation_flags.hpp:12-40). */
+enum { PI_VOLUME_ONLY = 1, PI_GRADIENT = 2, PI_HESSIAN = 4, PI_ALL = 7 };
+/* Contraction precision for V = Re(J^H diag(w) J). */
+enum {
+  PI_CONTRACT_FP32 = 0,      /* FP32 SIMT (the plain drop-in)                       */
+  PI_CONTRACT_BF16X3 = 1     /* BF16 hi+lo split on tcgen05 tensor cores, FP32 accum */
+};
+
+/* ---- packed element layouts (reference cpp/include/geometry/types.hpp:9-37) */
+typedef struct { double a[3], e1[3], e2[3], S[3]; int32_t vid0, vid1, vid2, pad_; } pi_tri_packed;     /* 112 B */
+typedef struct { double c[3], n[3]; double rho, area; } pi_disk_packed;                              /* 64 B  */
+typedef struct { double c[3], n[3]; double sigma, w; } pi_gaussian_packed;                           /* 64 B  */
+
+/* One object: packed elements + DoF parameterization + DoF vector.  AffineDoF
+ * vectors are [tx,ty,tz, A00..A22 row-major] (cpp/src/dof/affine_dof.cpp:17-29);
+ * TriangleMeshDoF vectors are 3V vertex coordinates indexed by vid0..2.
+ * Whether `elems` / `dofs` are host or device pointers is stated by each
+ * entry point. */
+typedef struct {
+  int32_t geom_type;
+  int32_t dof_type;
+  int64_t n_elems;
+  const void* elems;
+  int64_t n_dofs;
+  const double* dofs;
+} pi_object;
+
+/* ---- errors / version ------------------------------------------------------ */
+const char* pi_status_string(int status);
+const char* pi_last_error(void);
+int pi_version(void);
+/* Number of device-side launches the library issued on this thread (for
+ * instrumentation of benchmarks). */
+int64_t pi_launch_count(void);
+
+/* ---- host-side quadrature and geometry helpers (no GPU needed) ------------- */
+/* gauss_legendre_interval (cpp/include/quadrature/gauss_legendre.hpp:16-62) */
+int pi_gauss_legendre(int n, double a, double b, double* x, double* w);
+/* load_lebedev_txt (cpp/include/quadrature/lebedev_io.hpp:24-59); returns the
+ * row count in *n_rows and fills up to `cap` rows (dirs: cap x 3). */
+int pi_load_lebedev(const char* path, double* dirs, double* w, int64_t cap, int64_t* n_rows);
+/* build_kgrid (cpp/include/quadrature/kgrid.hpp:17-47); outputs Q = M*n_radial nodes. */
+int pi_build_kgrid(const double* leb_dirs, const double* leb_w, int64_t M, int n_radial,
+                   double* dirs, double* kmag, double* w);
+/* pack_tris / pack_disks / pack_gaussians (cpp/src/geometry/packing.cpp:10-112) */
+int pi_pack_tris(const double* V, int64_t n_verts, const int32_t* F, int64_t n_faces, pi_tri_packed* out);
+int pi_pack_disks(const double* P, const double* N, const double* radii_or_areas, int64_t n, int is_radius,
+                  pi_disk_packed* out);
+int pi_pack_gaussians(const double* P, const double* N, const double* sigmas, const double* weights, int64_t n,
+                      pi_gaussian_packed* out);
+/* create_unit_cube_mesh / create_sphere_pointcloud / create_sphere_gaussians
+ * (cpp/src/geometry/geometry_helpers.cpp:16-131) */
+int pi_create_unit_cube_mesh(double* V /*8x3*/, int32_t* F /*12x3*/);
+int pi_create_sphere_pointcloud(int n, double* P, double* N, double* radii);
+int pi_create_sphere_gaussians(int n, double* P, double* N, double* sigmas, double* weights);
+/* box_box / sphere_sphere_intersection_volume (cpp/src/analytical_intersection.cpp:15-60) */
+double pi_box_box_intersection_volume(const double* c1, const double* h1, const double* c2, const double* h2);
+double pi_sphere_sphere_intersection_volume(const double* c1, double r1, const double* c2, double r2);
+/* DoFParameterization::compute_volume -- divergence theorem (cpp/src/compute_volume.cpp:17-73,
+ * cpp/src/dof/affine_dof.cpp:324-384, cpp/src/dof/triangle_mesh_dof.cpp:145-179). Host object. */
+int pi_self_volume(const pi_object* obj, double* volume);
+
+/* ---- device-resident k-grid -------------------------------------------------- */
+/* Uploads a KGrid once (the reference re-uploaded it for every object on every
+ * call, cpp/src/dof/cuda/affine_dof_cuda.cu:895-914).  Host arrays.  A grid in
+ * the reference's tensor order (q = ir*M + j) is detected and stored factored
+ * as M directions x L radii; any other grid is stored node by node. */
+typedef struct pi_kgrid_s* pi_kgrid;
+int pi_kgrid_create(const double* dirs, const double* kmag, const double* w, int64_t Q, pi_kgrid* out);
+int pi_kgrid_destroy(pi_kgrid kg);
+int pi_kgrid_info(pi_kgrid kg, int64_t* Q, int64_t* n_dirs, int64_t* n_radial);
+
+/* ---- device-resident object batch ------------------------------------------- */
+/* A set of objects transformed by their DoFs into the kernels' FP32 local-frame
+ * layout.  `on_device` says whether elems/dofs in `objs` are device (1) or host
+ * (0) pointers; the batch keeps its own copies.  Replaces the per-object,
+ * per-call uploads of the reference's registry wrappers. */
+typedef struct pi_batch_s* pi_batch;
+int pi_batch_create(const pi_object* objs, int n_objects, int on_device, pi_stream stream, pi_batch* out);
+/* Replace the DoF vector of object `index` (device pointer, same length) and
+ * re-transform it, stream-ordered. */
+int pi_batch_set_dofs(pi_batch b, int index, const double* d_dofs, pi_stream stream);
+/* Re-run the DoF transform of every object from the batch's current DoF
+ * vectors (stream-ordered). */
+int pi_batch_prepare(pi_batch b, pi_stream stream);
+int pi_batch_destroy(pi_batch b);
+int pi_batch_count(pi_batch b, int* n_objects);
+
+/* ---- form factors: J[n][q] = A_n(k_q) (complex64, n_objects x Q) ------------ */
+/* Replaces kernels K1-K3, K7 and K12 (cpp/src/dof/cuda/affine_dof_cuda.cu:43-250,
+ * 580-689; cpp/src/dof/cuda/triangle_mesh_dof_cuda.cu:34-143;
+ * cpp/src/compute_intersection_volume_multi_object.cu:33-46).  If
+ * scale_sqrt_w != 0 every row q is multiplied by sqrt(|w_q|) (the contraction's
+ * operand form).  d_J: device, n_objects*Q*8 bytes. */
+int pi_form_factors(pi_kgrid kg, pi_batch b, int scale_sqrt_w, void* d_J, pi_stream stream);
+
+/* ---- contraction V = Re(J^H diag(w) J)/(8 pi^3) -------------------------------- */
+/* Replaces K9 and K14 (cpp/src/compute_intersection_volume.cu:33-50;
+ * cpp/src/compute_intersection_volume_multi_object.cu:74-116).  d_Jw is the
+ * sqrt(|w|)-scaled J from pi_form_factors(scale_sqrt_w=1).  d_V: device
+ * n x n doubles (full symmetric matrix).  d_ws: device workspace of at least
+ * the size reported by pi_contract_workspace_size. */
+int pi_contract_workspace_size(pi_kgrid kg, int n_objects, int precision, size_t* bytes);
+int pi_contract(pi_kgrid kg, const void* d_Jw, int n_objects, int precision, double* d_V, void* d_ws,
+                size_t ws_bytes, pi_stream stream);
+
+/* ---- one-shot host-buffer drop-ins ------------------------------------------ */
+/* compute_intersection_volume_matrix_cuda (cpp/include/compute_intersection_volume_multi_object.hpp:51-59).
+ * Host objects and k-grid; V_out: host n x n.  flags: PI_VOLUME_ONLY only in
+ * this entry point (gradients go through the adjoint entry points). */
+int pi_volume_matrix_host(const pi_object* objs, int n_objects, const double* dirs, const double* kmag,
+                          const double* w, int64_t Q, int flags, int precision, double* V_out);
+/* compute_intersection_volume_cuda (cpp/include/compute_intersection_volume.hpp:48-59), volume. */
+int pi_pair_volume_host(const pi_object* o1, const pi_object* o2, const double* dirs, const double* kmag,
+                        const double* w, int64_t Q, double* volume);
+/* CudaComputeAkFunc registry plugin (cpp/include/dof/cuda/dof_cuda_interface.hpp:24-30):
+ * host object and k-grid, output d_A_out = Q complex doubles (double2) on the device. */
+int pi_compute_Ak(const pi_object* obj, const double* dirs, const double* kmag, int64_t Q, double* d_A_out,
+                  int block_size);
+/* compute_Ak_cuda (cpp/include/compute_intersection_volume.hpp:120-126): A at one
+ * k-vector, host in and out (out = re, im). */
+int pi_compute_Ak_single(const pi_object* obj, const double* k, double* out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* POINTINT_GB300_H */

@@ -1,0 +1,113 @@
+"""ctypes binding to libpointint_gb300.so (the C ABI in include/pointint_gb300.h).
+
+There is no fallback: if the library is missing, importing the compute entry
+points raises.  Build it with ``python -m pointint_gb300.build`` or
+``__graft_entry__.build()``.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import threading
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libpointint_gb300.so")
+
+PI_OK = 0
+STATUS_NAMES = {0: "ok", 1: "invalid argument", 2: "CUDA error", 3: "unsupported", 4: "out of memory",
+                5: "not found", 6: "workspace too small", 7: "I/O error", 8: "timeout"}
+
+GEOM_TRIANGLE, GEOM_DISK, GEOM_GAUSSIAN = 0, 1, 2
+DOF_AFFINE, DOF_TRIANGLE_MESH = 0, 1
+VOLUME_ONLY, GRADIENT, HESSIAN, ALL = 1, 2, 4, 7
+CONTRACT_FP32, CONTRACT_BF16X3 = 0, 1
+
+
+class PointIntError(RuntimeError):
+    """A non-zero status from the C ABI."""
+
+    def __init__(self, status: int, message: str):
+        super().__init__(f"{STATUS_NAMES.get(status, status)}: {message}")
+        self.status = status
+
+
+class PiObject(ctypes.Structure):
+    """pi_object: packed elements + DoF type + DoF vector (host or device pointers)."""
+    _fields_ = [("geom_type", ctypes.c_int32), ("dof_type", ctypes.c_int32),
+                ("n_elems", ctypes.c_int64), ("elems", ctypes.c_void_p),
+                ("n_dofs", ctypes.c_int64), ("dofs", ctypes.c_void_p)]
+
+
+_lock = threading.Lock()
+_lib = None
+
+P, I32, I64, D, SZ = ctypes.c_void_p, ctypes.c_int, ctypes.c_int64, ctypes.c_double, ctypes.c_size_t
+PP = ctypes.POINTER(ctypes.c_void_p)
+OBJP = ctypes.POINTER(PiObject)
+
+# name -> (restype, argtypes); every symbol declared in include/pointint_gb300.h
+SIGNATURES = {
+    "pi_status_string": (ctypes.c_char_p, [I32]),
+    "pi_last_error": (ctypes.c_char_p, []),
+    "pi_version": (I32, []),
+    "pi_launch_count": (I64, []),
+    "pi_gauss_legendre": (I32, [I32, D, D, P, P]),
+    "pi_load_lebedev": (I32, [ctypes.c_char_p, P, P, I64, ctypes.POINTER(I64)]),
+    "pi_build_kgrid": (I32, [P, P, I64, I32, P, P, P]),
+    "pi_pack_tris": (I32, [P, I64, P, I64, P]),
+    "pi_pack_disks": (I32, [P, P, P, I64, I32, P]),
+    "pi_pack_gaussians": (I32, [P, P, P, P, I64, P]),
+    "pi_create_unit_cube_mesh": (I32, [P, P]),
+    "pi_create_sphere_pointcloud": (I32, [I32, P, P, P]),
+    "pi_create_sphere_gaussians": (I32, [I32, P, P, P, P]),
+    "pi_box_box_intersection_volume": (D, [P, P, P, P]),
+    "pi_sphere_sphere_intersection_volume": (D, [P, D, P, D]),
+    "pi_self_volume": (I32, [OBJP, ctypes.POINTER(D)]),
+    "pi_kgrid_create": (I32, [P, P, P, I64, PP]),
+    "pi_kgrid_destroy": (I32, [P]),
+    "pi_kgrid_info": (I32, [P, ctypes.POINTER(I64), ctypes.POINTER(I64), ctypes.POINTER(I64)]),
+    "pi_batch_create": (I32, [OBJP, I32, I32, P, PP]),
+    "pi_batch_set_dofs": (I32, [P, I32, P, P]),
+    "pi_batch_prepare": (I32, [P, P]),
+    "pi_batch_destroy": (I32, [P]),
+    "pi_batch_count": (I32, [P, ctypes.POINTER(I32)]),
+    "pi_form_factors": (I32, [P, P, I32, P, P]),
+    "pi_contract_workspace_size": (I32, [P, I32, I32, ctypes.POINTER(SZ)]),
+    "pi_contract": (I32, [P, P, I32, I32, P, P, SZ, P]),
+    "pi_volume_matrix_host": (I32, [OBJP, I32, P, P, P, I64, I32, I32, P]),
+    "pi_pair_volume_host": (I32, [OBJP, OBJP, P, P, P, I64, ctypes.POINTER(D)]),
+    "pi_compute_Ak": (I32, [OBJP, P, P, I64, P, I32]),
+    "pi_compute_Ak_single": (I32, [OBJP, P, P]),
+}
+
+
+def lib_exists() -> bool:
+    return os.path.exists(LIB_PATH)
+
+
+def lib() -> ctypes.CDLL:
+    """Load the library (no implicit build, no fallback)."""
+    global _lib
+    with _lock:
+        if _lib is None:
+            if not os.path.exists(LIB_PATH):
+                raise ImportError(
+                    f"{LIB_PATH} is missing: build it with `python -m pointint_gb300.build` "
+                    "(the GB300 path has no CPU fallback)")
+            L = ctypes.CDLL(LIB_PATH)
+            for name, (res, args) in SIGNATURES.items():
+                f = getattr(L, name)
+                f.restype = res
+                f.argtypes = args
+            _lib = L
+        return _lib
+
+
+def check(rc: int) -> None:
+    if rc != PI_OK:
+        msg = lib().pi_last_error()
+        raise PointIntError(rc, msg.decode() if msg else "")
+
+
+def launch_count() -> int:
+    return int(lib().pi_launch_count())

@@ -1,0 +1,173 @@
+// Device arithmetic for the FP32 form-factor kernels.
+//
+// Phases k.x reach 1e4-1e5 rad on the configs' k-grids (k up to ~7e3, centres
+// up to ~14 from the origin).  A plain FP32 phase would carry ~1e-2 rad of
+// error there, so phases are formed as double-float (hi + lo FP32 pair) products
+// and reduced modulo 2 pi by the Cody-Waite method (W. J. Cody and W. Waite,
+// "Software Manual for the Elementary Functions", 1980) with a two-part split
+// of 2 pi computed from its decimal expansion below, before the hardware
+// sin/cos is applied on [-pi, pi].  Error-free product / sum transformations
+// follow Dekker (1971) and Knuth (TAOCP vol. 2, 4.2.2).
+#pragma once
+#include <cuda_runtime.h>
+#include <cstdint>
+
+namespace pi {
+
+struct df { float hi, lo; };
+
+__device__ __forceinline__ df two_prod(float a, float b) {
+  float p = a * b;
+  return {p, fmaf(a, b, -p)};
+}
+
+__device__ __forceinline__ df two_sum(float a, float b) {
+  float s = a + b;
+  float bb = s - a;
+  float e = (a - (s - bb)) + (b - bb);
+  return {s, e};
+}
+
+__device__ __forceinline__ df quick_two_sum(float a, float b) {  // requires |a| >= |b|
+  float s = a + b;
+  return {s, b - (s - a)};
+}
+
+__device__ __forceinline__ df df_add(df a, df b) {
+  df s = two_sum(a.hi, b.hi);
+  return quick_two_sum(s.hi, s.lo + a.lo + b.lo);
+}
+
+__device__ __forceinline__ df df_mul(df a, df b) {
+  df p = two_prod(a.hi, b.hi);
+  float lo = fmaf(a.hi, b.lo, fmaf(a.lo, b.hi, p.lo));
+  return quick_two_sum(p.hi, lo);
+}
+
+__device__ __forceinline__ df df_scale(df a, float s) {  // a * s, s exact
+  df p = two_prod(a.hi, s);
+  return quick_two_sum(p.hi, fmaf(a.lo, s, p.lo));
+}
+
+// (dh + dl) . x in double-float, x in FP32.
+__device__ __forceinline__ df cdot(float3 dh, float3 dl, float3 x) {
+  df p0 = two_prod(dh.x, x.x), p1 = two_prod(dh.y, x.y), p2 = two_prod(dh.z, x.z);
+  df s = two_sum(p0.hi, p1.hi);
+  df t = two_sum(s.hi, p2.hi);
+  float lo = s.lo + t.lo + p0.lo + p1.lo + p2.lo + (dl.x * x.x + dl.y * x.y + dl.z * x.z);
+  return quick_two_sum(t.hi, lo);
+}
+
+// 2 pi = 6.28318530717958647692528676655900576839...
+//   TWO_PI_A = FP32(2 pi)                      = 6.28318548202514648437500
+//   TWO_PI_B = FP32(2 pi - TWO_PI_A)           = -1.7484556025237907e-07
+// |2 pi - A - B| < 1e-14, so n * (2 pi - A - B) < 1e-9 for |n| < 1e5.
+#define PI_TWO_PI_A 6.28318548202514648437500f
+#define PI_TWO_PI_B (-1.7484556025237907e-07f)
+#define PI_INV_TWO_PI 0.15915494309189533577f
+
+// Reduces a double-float phase to r in about [-pi, pi] with absolute error
+// ~3e-7 rad for |x| < 2^17; fmaf(-n, A, x) is exact because the result has at
+// most 24 significant bits (n integer, ulp(A) = 2^-21).
+__device__ __forceinline__ float reduce_2pi(df x) {
+  float n = rintf(x.hi * PI_INV_TWO_PI);
+  float r = fmaf(-n, PI_TWO_PI_A, x.hi);
+  r = fmaf(-n, PI_TWO_PI_B, r);
+  return r + x.lo;
+}
+
+struct cf { float re, im; };
+
+__device__ __forceinline__ cf cis(df phase) {  // e^{i phase}
+  float r = reduce_2pi(phase);
+  float s, c;
+  __sincosf(r, &s, &c);
+  return {c, s};
+}
+
+__device__ __forceinline__ cf cmul(cf a, cf b) { return {a.re * b.re - a.im * b.im, a.re * b.im + a.im * b.re}; }
+__device__ __forceinline__ cf csub(cf a, cf b) { return {a.re - b.re, a.im - b.im}; }
+__device__ __forceinline__ cf cscale(cf a, float s) { return {a.re * s, a.im * s}; }
+
+// First divided difference of f(z) = e^{iz} at two points u, v = u + g, given
+// Pu = e^{iu}, Pv = e^{iv}.  Uses (Pv - Pu)/g for |g| >= 1/2 and otherwise the
+// cancellation-free form i e^{i(u+v)/2} sinc(g/2) with short Taylor series of
+// cos, sin and sinc on |g/2| < 1/4 (truncation < 1e-9).
+__device__ __forceinline__ cf dd1(cf Pu, cf Pv, float g) {
+  if (fabsf(g) >= 0.5f) {
+    float ig = __frcp_rn(g);
+    return cscale(csub(Pv, Pu), ig);
+  }
+  float x = 0.5f * g, x2 = x * x;
+  float c = fmaf(x2, fmaf(x2, fmaf(x2, -1.0f / 720.0f, 1.0f / 24.0f), -0.5f), 1.0f);
+  float sc = fmaf(x2, fmaf(x2, fmaf(x2, -1.0f / 5040.0f, 1.0f / 120.0f), -1.0f / 6.0f), 1.0f);  // sinc x
+  float s = x * sc;
+  // i * (c + i s) * sc = (-s sc) + i (c sc)
+  cf m = cmul(Pu, cf{c, s});
+  return {-m.im * sc, m.re * sc};
+}
+
+// Second divided difference of e^{iz} at the vertex phases pa, pb = pa + al,
+// pc = pa + be of a triangle, times -2: the triangle's e^{ik.a} Phi(al, be)
+// (Phi as in the reference's Triangle_Phi_ab, cpp/src/element_functions.cpp:63-70,
+// which equals -2 e[0, al, be] for e(z) = e^{iz}).
+//
+//  * spread D = max(|al|, |be|, |be-al|) < 2: Taylor series about the centroid
+//    phase pm (no cancellation):  e[..] = e^{i pm} sum_m i^{m+2} h_m / (m+2)!,
+//    h_m the complete homogeneous symmetric polynomials of the centred points
+//    (|centred point| <= 2D/3), h_m = -e2 h_{m-2} + e3 h_{m-3} (e1 = 0),
+//    truncated after h_12 (remainder < 1e-8).
+//  * otherwise: (f[R,Q] - f[P,R]) / (Q - P) with (P, Q) the pair of vertices
+//    with the largest gap (|Q-P| = D >= 2, so the subtraction loses at most a
+//    factor ~1/D of FP32 precision) and stable first differences.
+__device__ __forceinline__ cf tri_phi_phase(df sa, df sb, df sc, df sm, df k, float al, float be) {
+  float D = fmaxf(fmaxf(fabsf(al), fabsf(be)), fabsf(be - al));
+  if (D < 2.0f) {
+    cf P = cis(df_mul(k, sm));
+    float da = -(al + be) * (1.0f / 3.0f);
+    float db = al + da, dc = be + da;
+    float e2 = -0.5f * (da * da + db * db + dc * dc);
+    float e3 = da * db * dc;
+    float me2 = -e2;
+    float h2 = me2, h3 = e3;
+    float h4 = me2 * h2;
+    float h5 = fmaf(me2, h3, e3 * h2);
+    float h6 = fmaf(me2, h4, e3 * h3);
+    float h7 = fmaf(me2, h5, e3 * h4);
+    float h8 = fmaf(me2, h6, e3 * h5);
+    float h9 = fmaf(me2, h7, e3 * h6);
+    float h10 = fmaf(me2, h8, e3 * h7);
+    float h11 = fmaf(me2, h9, e3 * h8);
+    float h12 = fmaf(me2, h10, e3 * h9);
+    float sre = -0.5f + h2 * (1.0f / 24.0f) - h4 * (1.0f / 720.0f) + h6 * (1.0f / 40320.0f) -
+                h8 * (1.0f / 3628800.0f) + h10 * (1.0f / 479001600.0f) - h12 * (1.0f / 87178291200.0f);
+    float sim = h3 * (1.0f / 120.0f) - h5 * (1.0f / 5040.0f) + h7 * (1.0f / 362880.0f) -
+                h9 * (1.0f / 39916800.0f) + h11 * (1.0f / 6227020800.0f);
+    cf r = cmul(P, cf{sre, sim});
+    return {-2.0f * r.re, -2.0f * r.im};
+  }
+  cf Pa = cis(df_mul(k, sa)), Pb = cis(df_mul(k, sb)), Pc = cis(df_mul(k, sc));
+  float gab = al, gac = be, gbc = be - al;
+  cf fRQ, fPR;
+  float den;
+  if (fabsf(gab) >= fabsf(gac) && fabsf(gab) >= fabsf(gbc)) {
+    // P = a, Q = b, R = c
+    fRQ = dd1(Pc, Pb, -gbc);
+    fPR = dd1(Pa, Pc, gac);
+    den = gab;
+  } else if (fabsf(gac) >= fabsf(gbc)) {
+    // P = a, Q = c, R = b
+    fRQ = dd1(Pb, Pc, gbc);
+    fPR = dd1(Pa, Pb, gab);
+    den = gac;
+  } else {
+    // P = b, Q = c, R = a
+    fRQ = dd1(Pa, Pc, gac);
+    fPR = dd1(Pb, Pa, -gab);
+    den = gbc;
+  }
+  float s = -2.0f * __frcp_rn(den);
+  return {(fRQ.re - fPR.re) * s, (fRQ.im - fPR.im) * s};
+}
+
+}  // namespace pi

@@ -1,0 +1,363 @@
+// Per-object form factors A_n(k_q) on the device.
+//
+// Replaces the reference kernels K1-K3 (cpp/src/dof/cuda/affine_dof_cuda.cu:43-250,
+// 580-689) and K7 (cpp/src/dof/cuda/triangle_mesh_dof_cuda.cu:34-143), whose
+// grid was one CTA per k-node looping over every element in FP64 with a shared
+// memory tree reduction.  Here:
+//
+//  * prepare_*: each object's elements are transformed once per DoF change by
+//    its AffineDoF / TriangleMeshDoF into an FP32 object-local frame (origin =
+//    centroid of the transformed anchors); the origin phase e^{ik.o} is applied
+//    per output in double-float.
+//  * ff_kernel: one CTA = one object x (8 warps); a warp owns 32 directions
+//    (one per lane) x R radial nodes of the factored k-grid, so each element's
+//    direction dot products are formed once and reused for R radii.  Elements
+//    are staged through shared memory and read as broadcasts; accumulation
+//    stays in registers (no reduction across threads); each output element is
+//    written once, coalesced, in the contraction's operand layout.
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <algorithm>
+#include "pi_internal.h"
+#include "dfmath.cuh"
+
+namespace pi {
+
+namespace {
+
+struct TriSrc { double a[3], e1[3], e2[3], S[3]; int32_t vid0, vid1, vid2, pad; };
+struct SurfSrc { double c[3], n[3], p0, p1; };
+
+struct PrepObj {
+  int32_t geom_type, dof_type;
+  int64_t n_elems, n_dofs;
+  const unsigned char* src;
+  const double* dofs;
+  int64_t pool_off;
+};
+
+__device__ __forceinline__ void affine_apply(const double* d, const double* x, double* y, bool translate) {
+  for (int r = 0; r < 3; ++r) {
+    double v = d[3 + 3 * r] * x[0] + d[3 + 3 * r + 1] * x[1] + d[3 + 3 * r + 2] * x[2];
+    y[r] = translate ? v + d[r] : v;
+  }
+}
+
+// Anchor point of element e after the DoF transform (first vertex / centre).
+__device__ __forceinline__ void anchor(const PrepObj& o, int64_t e, double* y) {
+  if (o.geom_type == PI_GEOM_TRIANGLE) {
+    const TriSrc& t = reinterpret_cast<const TriSrc*>(o.src)[e];
+    if (o.dof_type == PI_DOF_TRIANGLE_MESH) {
+      int64_t nv = o.n_dofs / 3;
+      if (t.vid0 < 0 || t.vid0 >= nv) { y[0] = y[1] = y[2] = 0.0; return; }
+      y[0] = o.dofs[3 * t.vid0]; y[1] = o.dofs[3 * t.vid0 + 1]; y[2] = o.dofs[3 * t.vid0 + 2];
+    } else {
+      affine_apply(o.dofs, t.a, y, true);
+    }
+  } else {
+    const SurfSrc& s = reinterpret_cast<const SurfSrc*>(o.src)[e];
+    affine_apply(o.dofs, s.c, y, true);
+  }
+}
+
+// One CTA per object: fixed-order mean of the anchors (deterministic), plus
+// the object's A A^T for the surfel k' = A^T k rule.
+__global__ void prepare_origin_kernel(const PrepObj* objs, ObjDev* out, int only) {
+  const int oi = only >= 0 ? only : blockIdx.x;
+  const PrepObj o = objs[oi];
+  __shared__ double red[3][256];
+  double s[3] = {0.0, 0.0, 0.0};
+  int64_t valid = 0;
+  for (int64_t e = threadIdx.x; e < o.n_elems; e += blockDim.x) {
+    double y[3];
+    anchor(o, e, y);
+    s[0] += y[0]; s[1] += y[1]; s[2] += y[2];
+    ++valid;
+  }
+  for (int c = 0; c < 3; ++c) red[c][threadIdx.x] = s[c];
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w)
+      for (int c = 0; c < 3; ++c) red[c][threadIdx.x] += red[c][threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    ObjDev d;
+    double inv = o.n_elems > 0 ? 1.0 / (double)o.n_elems : 0.0;
+    for (int c = 0; c < 3; ++c) d.origin[c] = red[c][0] * inv;
+    if (o.dof_type == PI_DOF_AFFINE) {
+      const double* A = o.dofs + 3;
+      double M[3][3];
+      for (int r = 0; r < 3; ++r)
+        for (int c = 0; c < 3; ++c)
+          M[r][c] = A[3 * r] * A[3 * c] + A[3 * r + 1] * A[3 * c + 1] + A[3 * r + 2] * A[3 * c + 2];
+      d.Msym[0] = (float)M[0][0]; d.Msym[1] = (float)M[0][1]; d.Msym[2] = (float)M[0][2];
+      d.Msym[3] = (float)M[1][1]; d.Msym[4] = (float)M[1][2]; d.Msym[5] = (float)M[2][2];
+    } else {
+      d.Msym[0] = 1.f; d.Msym[1] = 0.f; d.Msym[2] = 0.f; d.Msym[3] = 1.f; d.Msym[4] = 0.f; d.Msym[5] = 1.f;
+    }
+    d.type = o.geom_type;
+    d.n_elems = (int32_t)o.n_elems;
+    d.elem_off = o.pool_off;
+    out[oi] = d;
+  }
+}
+
+// grid (x: element blocks, y: object).  Writes the FP32 local-frame pools.
+__global__ void prepare_elems_kernel(const PrepObj* objs, const ObjDev* od, float4* tri_pool, float4* surf_pool,
+                                     int only) {
+  const int oi = only >= 0 ? only : blockIdx.y;
+  const PrepObj o = objs[oi];
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= o.n_elems) return;
+  const double* org = od[oi].origin;
+  if (o.geom_type == PI_GEOM_TRIANGLE) {
+    const TriSrc& t = reinterpret_cast<const TriSrc*>(o.src)[e];
+    double a[3], e1[3], e2[3];
+    bool ok = true;
+    if (o.dof_type == PI_DOF_TRIANGLE_MESH) {
+      int64_t nv = o.n_dofs / 3;
+      ok = t.vid0 >= 0 && t.vid1 >= 0 && t.vid2 >= 0 && t.vid0 < nv && t.vid1 < nv && t.vid2 < nv;
+      if (ok) {
+        const double* v0 = o.dofs + 3 * t.vid0;
+        const double* v1 = o.dofs + 3 * t.vid1;
+        const double* v2 = o.dofs + 3 * t.vid2;
+        for (int c = 0; c < 3; ++c) { a[c] = v0[c]; e1[c] = v1[c] - v0[c]; e2[c] = v2[c] - v0[c]; }
+      }
+    } else {
+      affine_apply(o.dofs, t.a, a, true);
+      affine_apply(o.dofs, t.e1, e1, false);
+      affine_apply(o.dofs, t.e2, e2, false);
+    }
+    float4* dst = tri_pool + 3 * (o.pool_off + e);
+    if (!ok) {  // unset vertex ids contribute nothing (triangle_mesh_dof.cpp:44-45)
+      dst[0] = make_float4(0.f, 0.f, 0.f, 0.f); dst[1] = dst[0]; dst[2] = dst[0];
+      return;
+    }
+    double S[3] = {0.5 * (e1[1] * e2[2] - e1[2] * e2[1]), 0.5 * (e1[2] * e2[0] - e1[0] * e2[2]),
+                   0.5 * (e1[0] * e2[1] - e1[1] * e2[0])};
+    dst[0] = make_float4((float)(a[0] - org[0]), (float)(a[1] - org[1]), (float)(a[2] - org[2]), (float)S[0]);
+    dst[1] = make_float4((float)e1[0], (float)e1[1], (float)e1[2], (float)S[1]);
+    dst[2] = make_float4((float)e2[0], (float)e2[1], (float)e2[2], (float)S[2]);
+  } else {
+    const SurfSrc& s = reinterpret_cast<const SurfSrc*>(o.src)[e];
+    double c[3], n[3];
+    affine_apply(o.dofs, s.c, c, true);
+    affine_apply(o.dofs, s.n, n, false);  // n' = A n so that k'.n = k.(A n) with k' = A^T k
+    float4* dst = surf_pool + 2 * (o.pool_off + e);
+    dst[0] = make_float4((float)(c[0] - org[0]), (float)(c[1] - org[1]), (float)(c[2] - org[2]), (float)s.p0);
+    dst[1] = make_float4((float)n[0], (float)n[1], (float)n[2], (float)s.p1);
+  }
+}
+
+constexpr int FF_THREADS = 256;
+constexpr int FF_WARPS = FF_THREADS / 32;
+constexpr int FF_TILE = 256;  // elements staged per shared-memory tile
+
+// J1(x)/x for the disk's 2 area J1(rho r)/(rho r)
+// (reference Disk_J1_over_x, cpp/src/element_functions.cpp:100-109).
+__device__ __forceinline__ float j1_over_x(float x) {
+  if (x < 1e-3f) {
+    float x2 = x * x;
+    return fmaf(x2, fmaf(x2, 1.0f / 384.0f, -1.0f / 16.0f), 0.5f);
+  }
+  return j1f(x) / x;
+}
+
+template <int R>
+__global__ void __launch_bounds__(FF_THREADS, 2)
+ff_kernel(KGridDev kg, BatchDev b, float2* __restrict__ J, int scale_sqrt_w) {
+  const int oi = b.order[blockIdx.y];
+  const ObjDev od = b.objs[oi];
+  const int nrb = (kg.L + R - 1) / R;
+  const int ndt = (kg.M + 31) / 32;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int item = blockIdx.x * FF_WARPS + warp;
+  const int dt = item / nrb, rb = item - dt * nrb;
+  const int j = dt * 32 + lane;
+  const bool active = item < ndt * nrb && j < kg.M;
+
+  float3 dh = make_float3(0.f, 0.f, 0.f), dl = dh;
+  float inv_norm = 0.f, dnorm = 0.f;
+  if (active) {
+    float4 h = kg.dir_hi[j], l = kg.dir_lo[j];
+    dh = make_float3(h.x, h.y, h.z); dl = make_float3(l.x, l.y, l.z);
+    inv_norm = h.w; dnorm = l.w;
+  }
+  df km[R];
+#pragma unroll
+  for (int i = 0; i < R; ++i) {
+    int r = rb * R + i;
+    float2 k = (active && r < kg.L) ? kg.kmag[r] : make_float2(0.f, 0.f);
+    km[i] = df{k.x, k.y};
+  }
+  float acc_re[R], acc_im[R];
+#pragma unroll
+  for (int i = 0; i < R; ++i) { acc_re[i] = 0.f; acc_im[i] = 0.f; }
+
+  __shared__ float4 tile[3 * FF_TILE];
+  const int n = od.n_elems;
+
+  if (od.type == PI_GEOM_TRIANGLE) {
+    const float4* src = b.tri_pool + 3 * od.elem_off;
+    for (int base = 0; base < n; base += FF_TILE) {
+      const int cnt = min(FF_TILE, n - base);
+      __syncthreads();
+      for (int t = threadIdx.x; t < 3 * cnt; t += FF_THREADS) tile[t] = src[3 * (int64_t)base + t];
+      __syncthreads();
+      if (active) {
+        for (int e = 0; e < cnt; ++e) {
+          const float4 q0 = tile[3 * e], q1 = tile[3 * e + 1], q2 = tile[3 * e + 2];
+          const float3 a = make_float3(q0.x, q0.y, q0.z);
+          const float3 e1 = make_float3(q1.x, q1.y, q1.z);
+          const float3 e2 = make_float3(q2.x, q2.y, q2.z);
+          // gamma = khat . S  (times the -2 of Phi = -2 e[0,al,be] folded in tri_phi_phase)
+          const float g = (dh.x * q0.w + dh.y * q1.w + dh.z * q2.w) * inv_norm;
+          const df sa = cdot(dh, dl, a), s1 = cdot(dh, dl, e1), s2 = cdot(dh, dl, e2);
+          const df sb = df_add(sa, s1), sc = df_add(sa, s2);
+          const df sm = df_add(sa, df_scale(df_add(s1, s2), 1.0f / 3.0f));
+#pragma unroll
+          for (int i = 0; i < R; ++i) {
+            const float al = km[i].hi * s1.hi, be = km[i].hi * s2.hi;
+            const cf v = tri_phi_phase(sa, sb, sc, sm, km[i], al, be);
+            acc_re[i] = fmaf(g, v.re, acc_re[i]);
+            acc_im[i] = fmaf(g, v.im, acc_im[i]);
+          }
+        }
+      }
+    }
+  } else {
+    const float4* src = b.surf_pool + 2 * od.elem_off;
+    const bool disk = od.type == PI_GEOM_DISK;
+    // qd = dir^T (A A^T) dir, so |k'|^2 = kmag^2 qd
+    const float* Ms = od.Msym;
+    const float qd = dh.x * (Ms[0] * dh.x + Ms[1] * dh.y + Ms[2] * dh.z) +
+                     dh.y * (Ms[1] * dh.x + Ms[3] * dh.y + Ms[4] * dh.z) +
+                     dh.z * (Ms[2] * dh.x + Ms[4] * dh.y + Ms[5] * dh.z);
+    for (int base = 0; base < n; base += FF_TILE) {
+      const int cnt = min(FF_TILE, n - base);
+      __syncthreads();
+      for (int t = threadIdx.x; t < 2 * cnt; t += FF_THREADS) tile[t] = src[2 * (int64_t)base + t];
+      __syncthreads();
+      if (active) {
+        for (int e = 0; e < cnt; ++e) {
+          const float4 q0 = tile[2 * e], q1 = tile[2 * e + 1];
+          const df sc = cdot(dh, dl, make_float3(q0.x, q0.y, q0.z));
+          const float sn = dh.x * q1.x + dh.y * q1.y + dh.z * q1.z;  // dir . (A n)
+          const float perp = fmaxf(qd - sn * sn, 0.f);              // |k'_perp|^2 / kmag^2
+          const float amp = sn * inv_norm * q1.w;                   // area|w * (k'.n)/|k|
+          if (disk) {
+            const float rr = q0.w * sqrtf(perp);                    // rho |k'_perp| / kmag
+#pragma unroll
+            for (int i = 0; i < R; ++i) {
+              const float x = km[i].hi * rr;
+              const float S = (x < 1e-10f) ? 1.0f : 2.0f * j1_over_x(x);
+              const cf P = cis(df_mul(km[i], sc));
+              const float m = S * amp;
+              acc_re[i] = fmaf(m, P.re, acc_re[i]);
+              acc_im[i] = fmaf(m, P.im, acc_im[i]);
+            }
+          } else {
+            const float hs = -0.5f * q0.w * q0.w * perp;
+#pragma unroll
+            for (int i = 0; i < R; ++i) {
+              const float k2 = km[i].hi * km[i].hi;
+              const float m = __expf(hs * k2) * amp;
+              const cf P = cis(df_mul(km[i], sc));
+              acc_re[i] = fmaf(m, P.re, acc_re[i]);
+              acc_im[i] = fmaf(m, P.im, acc_im[i]);
+            }
+          }
+        }
+      }
+    }
+  }
+
+  if (!active) return;
+  // origin phase e^{i k.o}: dir . o formed in FP64 once per thread, then double-float.
+  const double dox = (double)dh.x + (double)dl.x, doy = (double)dh.y + (double)dl.y,
+               doz = (double)dh.z + (double)dl.z;
+  const double so_d = dox * od.origin[0] + doy * od.origin[1] + doz * od.origin[2];
+  const float so_h = (float)so_d;
+  const df so = df{so_h, (float)(so_d - (double)so_h)};
+  const int64_t Jrow = (int64_t)oi * kg.Q;
+#pragma unroll
+  for (int i = 0; i < R; ++i) {
+    const int r = rb * R + i;
+    if (r < kg.L) {
+      const int64_t q = (int64_t)r * kg.M + j;
+      cf v = cmul(cis(df_mul(km[i], so)), cf{acc_re[i], acc_im[i]});
+      if (km[i].hi * dnorm < 1e-10f) v = cf{0.f, 0.f};  // A(0) = 0 (affine_dof.cpp:64-65)
+      if (scale_sqrt_w) { const float s = kg.sqrtw[q]; v.re *= s; v.im *= s; }
+      J[Jrow + q] = make_float2(v.re, v.im);
+    }
+  }
+}
+
+__global__ void to_double2_kernel(const float2* __restrict__ J, int64_t n, double2* __restrict__ out) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) { float2 v = J[i]; out[i] = make_double2(v.x, v.y); }
+}
+
+}  // namespace
+
+int launch_prepare(pi_batch_impl* b, int only_index, cudaStream_t s) {
+  std::vector<PrepObj> h(b->n_obj);
+  int64_t max_elems = 0;
+  for (int i = 0; i < b->n_obj; ++i) {
+    const HostObjInfo& in = b->info[i];
+    PrepObj& p = h[i];
+    p.geom_type = in.geom_type; p.dof_type = in.dof_type; p.n_elems = in.n_elems; p.n_dofs = in.n_dofs;
+    p.src = static_cast<const unsigned char*>(b->d_src) + in.src_off;
+    p.dofs = b->d_dofs + in.dof_off;
+    p.pool_off = in.pool_off;
+    if (only_index < 0 || only_index == i) max_elems = std::max(max_elems, in.n_elems);
+  }
+  if (b->n_obj == 0) return PI_OK;
+  PrepObj* d = nullptr;
+  PI_CUDA(cudaMallocAsync((void**)&d, sizeof(PrepObj) * h.size(), s));
+  PI_CUDA(cudaMemcpyAsync(d, h.data(), sizeof(PrepObj) * h.size(), cudaMemcpyHostToDevice, s));
+  const int nobj_launch = only_index >= 0 ? 1 : b->n_obj;
+  prepare_origin_kernel<<<nobj_launch, 256, 0, s>>>(d, b->d_objs, only_index);
+  PI_LAUNCHED("prepare_origin_kernel");
+  if (max_elems > 0) {
+    dim3 grid((unsigned)((max_elems + 255) / 256), (unsigned)nobj_launch);
+    prepare_elems_kernel<<<grid, 256, 0, s>>>(d, b->d_objs, b->d_tri_pool, b->d_surf_pool, only_index);
+    PI_LAUNCHED("prepare_elems_kernel");
+  }
+  // The host staging array `h` has been consumed by the copy above once the
+  // stream reaches it; cudaMemcpyAsync from pageable memory is synchronous
+  // with respect to the host buffer, so it may go out of scope here.
+  PI_CUDA(cudaFreeAsync(d, s));
+  return PI_OK;
+}
+
+int launch_form_factors(const pi_kgrid_impl* kg, const pi_batch_impl* b, int scale_sqrt_w, float2* J,
+                        cudaStream_t s) {
+  if (b->n_obj == 0) return PI_OK;
+  const KGridDev K = kg->dev;
+  const BatchDev B = b->dev();
+  int R = K.L >= 128 ? 16 : K.L >= 32 ? 8 : K.L >= 4 ? 4 : 1;
+  const int nrb = (K.L + R - 1) / R;
+  const int ndt = (K.M + 31) / 32;
+  const int64_t items = (int64_t)nrb * ndt;
+  dim3 grid((unsigned)((items + FF_WARPS - 1) / FF_WARPS), (unsigned)b->n_obj);
+  if (grid.y > 65535) return fail(PI_ERR_UNSUPPORTED, "more than 65535 objects in one batch");
+  switch (R) {
+    case 16: ff_kernel<16><<<grid, FF_THREADS, 0, s>>>(K, B, J, scale_sqrt_w); break;
+    case 8: ff_kernel<8><<<grid, FF_THREADS, 0, s>>>(K, B, J, scale_sqrt_w); break;
+    case 4: ff_kernel<4><<<grid, FF_THREADS, 0, s>>>(K, B, J, scale_sqrt_w); break;
+    default: ff_kernel<1><<<grid, FF_THREADS, 0, s>>>(K, B, J, scale_sqrt_w); break;
+  }
+  PI_LAUNCHED("ff_kernel");
+  return PI_OK;
+}
+
+int launch_to_double2(const float2* J, int64_t n, double* out, cudaStream_t s) {
+  if (n == 0) return PI_OK;
+  to_double2_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(J, n, reinterpret_cast<double2*>(out));
+  PI_LAUNCHED("to_double2_kernel");
+  return PI_OK;
+}
+
+}  // namespace pi

@@ -1,0 +1,118 @@
+// Internal structures shared by the translation units of libpointint_gb300.
+#pragma once
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <string>
+#include <vector>
+#include "pointint_gb300.h"
+
+namespace pi {
+
+// ---- error handling ---------------------------------------------------------
+void set_error(const std::string& msg);
+int fail(int status, const std::string& msg);
+int cuda_fail(cudaError_t e, const char* what);
+void count_launch(int n = 1);
+
+#define PI_CUDA(call)                                        \
+  do {                                                       \
+    cudaError_t e_ = (call);                                 \
+    if (e_ != cudaSuccess) return ::pi::cuda_fail(e_, #call); \
+  } while (0)
+
+#define PI_LAUNCHED(what)                                           \
+  do {                                                              \
+    cudaError_t e_ = cudaGetLastError();                            \
+    if (e_ != cudaSuccess) return ::pi::cuda_fail(e_, what);        \
+    ::pi::count_launch();                                           \
+  } while (0)
+
+// ---- device k-grid ------------------------------------------------------------
+// Factored layout: node q = r * M + j has k_q = kmag[r] * dir[j].  Directions
+// are stored as FP32 hi/lo pairs so that phases k.x can be formed to ~2^-44
+// relative accuracy; radii likewise.  A grid without tensor structure is
+// stored with M = Q, L = 1, dir[j] = k_j and kmag = 1.
+struct KGridDev {
+  int64_t Q;
+  int M, L;
+  const float4* dir_hi;   // M: (hx, hy, hz, 1/|dir|)
+  const float4* dir_lo;   // M: (lx, ly, lz, |dir|)
+  const float2* kmag;     // L: (hi, lo)
+  const float* sqrtw;     // Q: sqrt(|w_q|)
+  const float* sign;      // Q: sign(w_q), or nullptr when every weight is >= 0
+};
+
+struct pi_kgrid_impl {
+  KGridDev dev;
+  void* d_mem = nullptr;        // single allocation behind the pointers above
+  std::vector<double> w;        // host copy of weights
+  int64_t Q = 0;
+  int M = 0, L = 0;
+  bool tensor = false;
+  bool all_positive = true;
+};
+
+// ---- device object batch -----------------------------------------------------
+struct ObjDev {
+  double origin[3];       // local-frame origin (transformed element centroid)
+  float Msym[6];          // A A^T (xx, xy, xz, yy, yz, zz) for disks/Gaussians
+  int32_t type;           // PI_GEOM_*
+  int32_t n_elems;
+  int64_t elem_off;       // offset (in elements) into the pool of its type
+};
+
+// Pools in the kernels' layout, object-local frame, FP32:
+//   triangles: 3 x float4 per element  (a.xyz, S.x) (e1.xyz, S.y) (e2.xyz, S.z)
+//   disks/Gaussians: 2 x float4        (c.xyz, rho|sigma) (n'.xyz, area|w)
+struct BatchDev {
+  int n_obj;
+  const ObjDev* objs;
+  const int32_t* order;      // CTA y-index -> object (largest first)
+  const float4* tri_pool;
+  const float4* surf_pool;
+};
+
+struct HostObjInfo {
+  int32_t geom_type, dof_type;
+  int64_t n_elems, n_dofs;
+  int64_t src_off;           // byte offset of its packed source in the source arena
+  int64_t dof_off;           // offset (doubles) into the dof arena
+  int64_t pool_off;          // element offset in its pool
+};
+
+struct pi_batch_impl {
+  int n_obj = 0;
+  std::vector<HostObjInfo> info;
+  std::vector<int32_t> order;
+  int64_t n_tri = 0, n_surf = 0;
+  // device allocations
+  void* d_src = nullptr;     // packed reference-layout elements of all objects
+  double* d_dofs = nullptr;  // all DoF vectors
+  float4* d_tri_pool = nullptr;
+  float4* d_surf_pool = nullptr;
+  ObjDev* d_objs = nullptr;
+  int32_t* d_order = nullptr;
+  BatchDev dev() const {
+    BatchDev b;
+    b.n_obj = n_obj; b.objs = d_objs; b.order = d_order; b.tri_pool = d_tri_pool; b.surf_pool = d_surf_pool;
+    return b;
+  }
+};
+
+// ---- launchers (formfactor.cu / contract.cu) ------------------------------------
+int launch_prepare(pi_batch_impl* b, int only_index, cudaStream_t s);
+int launch_form_factors(const pi_kgrid_impl* kg, const pi_batch_impl* b, int scale_sqrt_w, float2* J,
+                        cudaStream_t s);
+size_t contract_fp32_ws_bytes(int64_t Q, int n);
+int launch_contract_fp32(const pi_kgrid_impl* kg, const float2* Jw, int n, double* V, void* ws, size_t ws_bytes,
+                         cudaStream_t s);
+size_t contract_tc_ws_bytes(int64_t Q, int n);
+int launch_contract_tc(const pi_kgrid_impl* kg, const float2* Jw, int n, double* V, void* ws, size_t ws_bytes,
+                       cudaStream_t s);
+int launch_pair_dot(const pi_kgrid_impl* kg, const float2* Jw, double* d_out, void* ws, cudaStream_t s);
+int launch_to_double2(const float2* J, int64_t n, double* out, cudaStream_t s);
+
+}  // namespace pi
+
+struct pi_kgrid_s : pi::pi_kgrid_impl {};
+struct pi_batch_s : pi::pi_batch_impl {};
