@@ -49,6 +49,8 @@ def parse():
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--cpu-seconds", type=float, default=12.0)
+    p.add_argument("--objects", type=int, default=256,
+                   help="object count of the matrix workload (256 = the benchmark; smaller only for profiling)")
     return p.parse_args()
 
 
@@ -186,7 +188,7 @@ def run_gb300(args):
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     from pointint_gb300 import configs, core, _lib
     peaks, peak_src = load_peaks()
-    kg, objs, meta = configs.matrix256(seed=rank)
+    kg, objs, meta = configs.matrix256(seed=rank, n_objects=args.objects)
     n_obj = len(objs)
     n_tri = meta["n_triangles"]
     Q = kg.num_nodes

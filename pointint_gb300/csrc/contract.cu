@@ -6,8 +6,9 @@
 // X = [Re sqrt|w| J ; Im sqrt|w| J] (n x 2Q real, the layout the form-factor
 // kernel writes), V is the SYRK X diag(sign) X^T.  Upper-triangle 64x64 output
 // tiles x split-K; each thread owns a 4x4 register block and sums every 32-wide
-// K slab into a fresh block before adding it to its running sum (two-level
-// summation keeps FP32 error near sqrt(K) eps).  Per-split partial tiles are
+// K slab into a fresh block before adding it, Kahan-compensated, to its
+// running sum (off-diagonal entries are small differences of large slab sums).
+// Per-split partial tiles are
 // reduced in a fixed order in FP64 by a second kernel: results are bitwise
 // reproducible run to run.
 #include <cuda_runtime.h>
@@ -51,11 +52,11 @@ syrk_fp32_kernel(const float* __restrict__ X, int n, int64_t K, const float* __r
   __shared__ __align__(16) float Bs[KT][TB + PAD];
   const int tid = threadIdx.x, ty = tid >> 4, tx = tid & 15;
   const bool vec = (K & 3) == 0;
-  float acc[4][4];
+  float acc[4][4], cmp[4][4];  // running sum + Kahan compensation
 #pragma unroll
   for (int a = 0; a < 4; ++a)
 #pragma unroll
-    for (int c = 0; c < 4; ++c) acc[a][c] = 0.f;
+    for (int c = 0; c < 4; ++c) { acc[a][c] = 0.f; cmp[a][c] = 0.f; }
 
   for (int64_t k = k0; k < k1; k += KT) {
 #pragma unroll
@@ -92,7 +93,12 @@ syrk_fp32_kernel(const float* __restrict__ X, int n, int64_t K, const float* __r
 #pragma unroll
     for (int a = 0; a < 4; ++a)
 #pragma unroll
-      for (int c = 0; c < 4; ++c) acc[a][c] += part[a][c];
+      for (int c = 0; c < 4; ++c) {  // Kahan: the slab sums of an off-diagonal entry cancel
+        const float y = part[a][c] - cmp[a][c];
+        const float t = acc[a][c] + y;
+        cmp[a][c] = (t - acc[a][c]) - y;
+        acc[a][c] = t;
+      }
     __syncthreads();
   }
   float* out = partials + ((int64_t)blockIdx.y * gridDim.x + blockIdx.x) * (TB * TB);

@@ -1,13 +1,344 @@
-// Volume contraction on tcgen05 tensor cores (BF16 hi+lo split, FP32 accumulation).
+// Volume contraction on tcgen05 tensor cores: BF16 hi+lo split, FP32 accumulation.
+//
+// V = X X^T with X = [Re sqrt|w| J ; Im sqrt|w| J] (n x 2Q, the FP32 layout the
+// form-factor kernel writes).  Each FP32 operand value x is split into
+// h = bf16(x) and l = bf16(x - h) while it is staged, and every output tile
+// accumulates  H_i H_j^T + H_i L_j^T + L_i H_j^T  (the l.l term, ~2^-16
+// relative, is dropped) in a 128x128 FP32 accumulator in tensor memory.
+//
+// CTA = 8 producer warps + 1 MMA warp.  Work unit = (upper-triangle pair of
+// 128-row object blocks, K range).  Producers load 8 FP32 values per thread
+// per step (coalesced 32-byte rows), split them, and store both halves into a
+// 3-stage ring of 128-byte-swizzled K-major tiles (the canonical layout of
+// the UMMA shared-memory descriptors); an elected thread of the MMA warp
+// issues tcgen05.mma (M = N = 128, K = 16) three times per K step and commits
+// each stage back to the producers through an mbarrier.  The epilogue reads
+// the accumulator with tcgen05.ld and writes a per-unit FP32 partial tile;
+// a second kernel sums the partials in a fixed order in FP64.
+//
+// Every wait is bounded (~2 s of SM clock); on expiry the kernel records an
+// error code in the workspace, stops issuing work, drains its outstanding
+// MMAs, frees its tensor memory and returns; the reduction then writes NaN to
+// V so a failure can never read as a volume.
 #include <cuda_runtime.h>
+#include <cuda_bf16.h>
+#include <cstdint>
+#include <algorithm>
 #include "pi_internal.h"
 
 namespace pi {
 
-size_t contract_tc_ws_bytes(int64_t, int) { return 0; }
+namespace {
 
-int launch_contract_tc(const pi_kgrid_impl*, const float2*, int, double*, void*, size_t, cudaStream_t) {
-  return fail(PI_ERR_UNSUPPORTED, "tensor-core contraction not built yet");
+constexpr int TC_M = 128;                       // tile edge (objects)
+constexpr int TC_KC = 64;                       // K elements per stage = one 128-byte bf16 row
+constexpr int TC_STAGES = 3;
+constexpr int TC_PWARPS = 8;                    // producer warps
+constexpr int TC_THREADS = (TC_PWARPS + 1) * 32;
+constexpr int BLK_BYTES = TC_M * TC_KC * 2;     // 16 KB: one bf16 operand block
+constexpr int STAGE_BYTES = 4 * BLK_BYTES;      // A hi, A lo, B hi, B lo
+constexpr int SMEM_BYTES = TC_STAGES * STAGE_BYTES + 1024;  // + alignment slack
+constexpr long long WAIT_CYCLES = 4000000000LL; // ~2 s at 2 GHz
+constexpr double INV8PI3 = 1.0 / (8.0 * 3.14159265358979323846 * 3.14159265358979323846 * 3.14159265358979323846);
+
+// kind::f16 instruction descriptor: D = F32 (bits 4-5 = 1), A = B = BF16
+// (bits 7-9 = 1, 10-12 = 1), both K-major, N >> 3 at bits 17-22, M >> 4 at 24-28.
+constexpr uint32_t IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(TC_M >> 3) << 17) |
+                           ((uint32_t)(TC_M >> 4) << 24);
+
+enum { ERR_PRODUCER_WAIT = 1, ERR_MMA_WAIT = 2, ERR_EPILOGUE_WAIT = 3 };
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+  asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.shared::cta.b64 st, [%0];\n\t}" ::"r"(bar) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(bar), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// Bounded wait for the completion of the barrier phase with the given parity.
+// Returns false (after recording `code`) on expiry, or at once if another
+// thread of the grid has already recorded an error.
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, int* err, int code) {
+  const long long t0 = clock64();
+  while (!mbar_try_wait(bar, parity)) {
+    if (*reinterpret_cast<volatile int*>(err) != 0) return false;
+    if (clock64() - t0 > WAIT_CYCLES) {
+      atomicCAS(err, 0, code);
+      return false;
+    }
+  }
+  return true;
+}
+
+__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+__device__ __forceinline__ void fence_mbar_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+// Shared-memory matrix descriptor, K-major, 128-byte swizzle: start address
+// (>>4, bits 0-13), leading byte offset (unused for this layout, 16 B),
+// stride byte offset 1024 B between 8-row swizzle atoms (bits 32-45),
+// descriptor version 1 (bits 46-48), swizzle mode 2 = 128 B (bits 61-63).
+__device__ __forceinline__ uint64_t desc_sw128(uint32_t saddr) {
+  uint64_t d = (uint64_t)((saddr & 0x3FFFFu) >> 4);
+  d |= (uint64_t)1 << 16;
+  d |= (uint64_t)(1024 >> 4) << 32;
+  d |= (uint64_t)1 << 46;
+  d |= (uint64_t)2 << 61;
+  return d;
+}
+
+__device__ __forceinline__ void umma_bf16(uint32_t tmem_d, uint64_t a, uint64_t b, uint32_t accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %3, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %4, p;\n\t}" ::"r"(tmem_d),
+      "l"(a), "l"(b), "r"(accumulate), "r"(IDESC)
+      : "memory");
+}
+
+__device__ __forceinline__ void umma_commit(uint32_t bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
+}
+
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float* v) {
+  uint32_t r[32];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, "
+      "%16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]),
+        "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
+        "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+__device__ __forceinline__ void tile_of(int p, int nt, int* bi, int* bj) {
+  int i = 0, rem = p;
+  while (rem >= nt - i) { rem -= nt - i; ++i; }
+  *bi = i; *bj = i + rem;
+}
+
+__device__ __forceinline__ uint32_t pack_bf16(float a, float b) {
+  __nv_bfloat162 v = __floats2bfloat162_rn(a, b);
+  return *reinterpret_cast<uint32_t*>(&v);
+}
+
+// Split 8 consecutive FP32 values into bf16 hi / lo halves (16 B each).
+__device__ __forceinline__ void split8(const float* x, uint4* hi, uint4* lo) {
+  float h[8], l[8];
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    h[i] = __bfloat162float(__float2bfloat16_rn(x[i]));
+    l[i] = x[i] - h[i];
+  }
+  *hi = make_uint4(pack_bf16(h[0], h[1]), pack_bf16(h[2], h[3]), pack_bf16(h[4], h[5]), pack_bf16(h[6], h[7]));
+  *lo = make_uint4(pack_bf16(l[0], l[1]), pack_bf16(l[2], l[3]), pack_bf16(l[4], l[5]), pack_bf16(l[6], l[7]));
+}
+
+__global__ void __launch_bounds__(TC_THREADS, 1)
+syrk_bf16x3_kernel(const float* __restrict__ X, int n, int64_t K, int nt, int64_t nchunks, int64_t cps,
+                   float* __restrict__ partials, int* __restrict__ err) {
+  extern __shared__ uint8_t smem_raw[];
+  __shared__ __align__(8) uint64_t full_bar[TC_STAGES];
+  __shared__ __align__(8) uint64_t empty_bar[TC_STAGES];
+  __shared__ __align__(8) uint64_t done_bar;
+  __shared__ uint32_t tmem_slot;
+
+  uint8_t* smem = smem_raw + ((1024 - (smem_u32(smem_raw) & 1023)) & 1023);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  int bi, bj;
+  tile_of(blockIdx.x, nt, &bi, &bj);
+  const bool diag = bi == bj;
+  const int64_t c0 = (int64_t)blockIdx.y * cps;
+  const int64_t nc = max((int64_t)0, min(nchunks, c0 + cps) - c0);
+
+  if (tid == 0) {
+    for (int s = 0; s < TC_STAGES; ++s) {
+      mbar_init(smem_u32(&full_bar[s]), TC_PWARPS);
+      mbar_init(smem_u32(&empty_bar[s]), 1);
+    }
+    mbar_init(smem_u32(&done_bar), 1);
+    fence_mbar_init();
+  }
+  if (warp == TC_PWARPS) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_slot)),
+                 "r"(TC_M));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = tmem_slot;
+
+  if (warp < TC_PWARPS) {
+    // ---------------- producers: FP32 -> bf16 hi/lo, swizzled K-major tiles ----------------
+    const int units = diag ? TC_M * 8 : 2 * TC_M * 8;  // 8-element units per stage
+    const bool vec = (K & 3) == 0;
+    for (int64_t c = 0; c < nc; ++c) {
+      const int s = (int)(c % TC_STAGES);
+      const int64_t r = c / TC_STAGES;
+      if (r > 0 && !mbar_wait(smem_u32(&empty_bar[s]), (uint32_t)((r - 1) & 1), err, ERR_PRODUCER_WAIT)) break;
+      uint8_t* st = smem + s * STAGE_BYTES;
+      const int64_t kbase = (c0 + c) * TC_KC;
+      for (int u = tid; u < units; u += TC_PWARPS * 32) {
+        const int blk = u >= TC_M * 8;
+        const int uu = u - blk * TC_M * 8;
+        const int row = uu >> 3, ch = uu & 7;
+        const int grow = (blk ? bj : bi) * TC_M + row;
+        const int64_t kk = kbase + ch * 8;
+        float x[8];
+        if (vec && grow < n && kk + 8 <= K) {  // 16-byte aligned: K % 4 == 0 and kk % 8 == 0
+          const float4* src = reinterpret_cast<const float4*>(X + (int64_t)grow * K + kk);
+          const float4 a = __ldg(src), b = __ldg(src + 1);
+          x[0] = a.x; x[1] = a.y; x[2] = a.z; x[3] = a.w; x[4] = b.x; x[5] = b.y; x[6] = b.z; x[7] = b.w;
+        } else {
+#pragma unroll
+          for (int i = 0; i < 8; ++i) x[i] = (grow < n && kk + i < K) ? X[(int64_t)grow * K + kk + i] : 0.f;
+        }
+        uint4 hi, lo;
+        split8(x, &hi, &lo);
+        const uint32_t off = (uint32_t)((row >> 3) * 1024 + (row & 7) * 128 + ((ch ^ (row & 7)) << 4));
+        uint8_t* base = st + (blk ? 2 * BLK_BYTES : 0);
+        *reinterpret_cast<uint4*>(base + off) = hi;
+        *reinterpret_cast<uint4*>(base + BLK_BYTES + off) = lo;
+      }
+      fence_proxy_async();
+      __syncwarp();
+      if (lane == 0) mbar_arrive(smem_u32(&full_bar[s]));
+    }
+  } else if (lane == 0) {
+    // ---------------- MMA issuer ----------------
+    for (int64_t c = 0; c < nc; ++c) {
+      const int s = (int)(c % TC_STAGES);
+      const int64_t r = c / TC_STAGES;
+      if (!mbar_wait(smem_u32(&full_bar[s]), (uint32_t)(r & 1), err, ERR_MMA_WAIT)) break;
+      tc_fence_after();
+      const uint32_t st = smem_u32(smem + s * STAGE_BYTES);
+      const uint64_t aH = desc_sw128(st), aL = desc_sw128(st + BLK_BYTES);
+      const uint64_t bH = diag ? aH : desc_sw128(st + 2 * BLK_BYTES);
+      const uint64_t bL = diag ? aL : desc_sw128(st + 3 * BLK_BYTES);
+#pragma unroll
+      for (int k = 0; k < TC_KC / 16; ++k) {
+        const uint64_t adv = (uint64_t)(k * 32) >> 4;  // +32 bytes along K inside the swizzled row
+        umma_bf16(tmem, aH + adv, bH + adv, (c > 0 || k > 0) ? 1u : 0u);
+        umma_bf16(tmem, aH + adv, bL + adv, 1u);
+        umma_bf16(tmem, aL + adv, bH + adv, 1u);
+      }
+      umma_commit(smem_u32(&empty_bar[s]));
+    }
+    umma_commit(smem_u32(&done_bar));  // arrives once every issued MMA has completed
+  }
+
+  // ---------------- epilogue: TMEM -> FP32 partial tile ----------------
+  if (warp < 4) {
+    const bool ok = mbar_wait(smem_u32(&done_bar), 0u, err, ERR_EPILOGUE_WAIT);
+    tc_fence_after();
+    const int row = warp * 32 + lane;
+    float* out = partials + ((int64_t)blockIdx.y * gridDim.x + blockIdx.x) * (TC_M * TC_M) + (int64_t)row * TC_M;
+#pragma unroll 1
+    for (int cb = 0; cb < TC_M / 32; ++cb) {
+      float v[32];
+      if (ok && nc > 0) {
+        tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(cb * 32), v);
+      } else {
+#pragma unroll
+        for (int i = 0; i < 32; ++i) v[i] = 0.f;
+      }
+#pragma unroll
+      for (int i = 0; i < 32; i += 4)
+        *reinterpret_cast<float4*>(out + cb * 32 + i) = make_float4(v[i], v[i + 1], v[i + 2], v[i + 3]);
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == TC_PWARPS) {
+    __syncwarp();
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TC_M));
+  }
+}
+
+__global__ void reduce_tc_tiles_kernel(const float* __restrict__ partials, int nsplit, int npairs, int nt, int n,
+                                       const int* __restrict__ err, double* __restrict__ V) {
+  const int p = blockIdx.x;
+  int bi, bj;
+  tile_of(p, nt, &bi, &bj);
+  const bool bad = *err != 0;
+  for (int e = threadIdx.x; e < TC_M * TC_M; e += blockDim.x) {
+    const int r = e / TC_M, c = e % TC_M;
+    const int i = bi * TC_M + r, j = bj * TC_M + c;
+    if (i >= n || j >= n || (bi == bj && r > c)) continue;
+    double s = 0.0;
+    for (int sp = 0; sp < nsplit; ++sp) s += (double)partials[((int64_t)sp * npairs + p) * (TC_M * TC_M) + e];
+    s = bad ? __longlong_as_double(0x7ff8000000000000LL) : s * INV8PI3;
+    V[(int64_t)i * n + j] = s;
+    V[(int64_t)j * n + i] = s;
+  }
+}
+
+struct TcPlan { int nt, npairs, nsplit; int64_t K, nchunks, cps; };
+
+TcPlan plan_tc(int64_t Q, int n) {
+  TcPlan p;
+  p.K = 2 * Q;
+  p.nt = (n + TC_M - 1) / TC_M;
+  p.npairs = p.nt * (p.nt + 1) / 2;
+  p.nchunks = (p.K + TC_KC - 1) / TC_KC;
+  int dev = 0, sms = 148;
+  if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  int64_t nsplit = std::max<int64_t>(1, sms / p.npairs);
+  nsplit = std::min<int64_t>(nsplit, p.nchunks);
+  p.cps = (p.nchunks + nsplit - 1) / nsplit;
+  p.nsplit = (int)((p.nchunks + p.cps - 1) / p.cps);
+  return p;
+}
+
+}  // namespace
+
+size_t contract_tc_ws_bytes(int64_t Q, int n) {
+  if (n <= 0 || Q <= 0) return 0;
+  TcPlan p = plan_tc(Q, n);
+  return 256 + (size_t)p.nsplit * p.npairs * TC_M * TC_M * sizeof(float);
+}
+
+int launch_contract_tc(const pi_kgrid_impl* kg, const float2* Jw, int n, double* V, void* ws, size_t ws_bytes,
+                       cudaStream_t s) {
+  if (n <= 0) return PI_OK;
+  TcPlan p = plan_tc(kg->Q, n);
+  const size_t need = 256 + (size_t)p.nsplit * p.npairs * TC_M * TC_M * sizeof(float);
+  if (ws_bytes < need || !ws) return fail(PI_ERR_WORKSPACE_TOO_SMALL, "tensor-core contraction workspace too small");
+  if ((reinterpret_cast<uintptr_t>(Jw) & 15) != 0) return fail(PI_ERR_INVALID_ARGUMENT, "J must be 16-byte aligned");
+  static bool attr_set = false;
+  if (!attr_set) {
+    PI_CUDA(cudaFuncSetAttribute(syrk_bf16x3_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
+    attr_set = true;
+  }
+  int* err = static_cast<int*>(ws);
+  float* partials = reinterpret_cast<float*>(static_cast<unsigned char*>(ws) + 256);
+  PI_CUDA(cudaMemsetAsync(err, 0, sizeof(int), s));
+  dim3 grid((unsigned)p.npairs, (unsigned)p.nsplit);
+  syrk_bf16x3_kernel<<<grid, TC_THREADS, SMEM_BYTES, s>>>(reinterpret_cast<const float*>(Jw), n, p.K, p.nt,
+                                                         p.nchunks, p.cps, partials, err);
+  PI_LAUNCHED("syrk_bf16x3_kernel");
+  reduce_tc_tiles_kernel<<<p.npairs, 256, 0, s>>>(partials, p.nsplit, p.npairs, p.nt, n, err, V);
+  PI_LAUNCHED("reduce_tc_tiles_kernel");
+  return PI_OK;
 }
 
 }  // namespace pi

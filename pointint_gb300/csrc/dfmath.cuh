@@ -44,6 +44,10 @@ __device__ __forceinline__ df df_mul(df a, df b) {
   return quick_two_sum(p.hi, lo);
 }
 
+__device__ __forceinline__ df operator*(df a, float s) {  // a * s for s = +-1 or a power of two
+  return {a.hi * s, a.lo * s};
+}
+
 __device__ __forceinline__ df df_scale(df a, float s) {  // a * s, s exact
   df p = two_prod(a.hi, s);
   return quick_two_sum(p.hi, fmaf(a.lo, s, p.lo));
@@ -107,66 +111,71 @@ __device__ __forceinline__ cf dd1(cf Pu, cf Pv, float g) {
   return {-m.im * sc, m.re * sc};
 }
 
-// Second divided difference of e^{iz} at the vertex phases pa, pb = pa + al,
-// pc = pa + be of a triangle, times -2: the triangle's e^{ik.a} Phi(al, be)
-// (Phi as in the reference's Triangle_Phi_ab, cpp/src/element_functions.cpp:63-70,
-// which equals -2 e[0, al, be] for e(z) = e^{iz}).
+// Exact-ish division of a double-float by 3 (the FP32 quotient's remainder is
+// formed exactly with an FMA).
+__device__ __forceinline__ df df_div3(df a) {
+  const float q = a.hi * (1.0f / 3.0f);
+  const float r = fmaf(-q, 3.0f, a.hi);
+  return quick_two_sum(q, (r + a.lo) * (1.0f / 3.0f));
+}
+
+// The triangle form factor is e^{ik.a} Phi(al, be) (k.S)/|k| with Phi as in the
+// reference's Triangle_Phi_ab (cpp/src/element_functions.cpp:63-70), and
+// Phi = -2 e[0, al, be] for the divided differences e[..] of e(z) = e^{iz}.
+// Shifting by the vertex phase, e^{ik.a} Phi = -2 e[pa, pb, pc] with the vertex
+// phases pa = k.a, pb = k.b, pc = k.c.  Two evaluations are used, both without
+// the common factor -2:
 //
-//  * spread D = max(|al|, |be|, |be-al|) < 2: Taylor series about the centroid
-//    phase pm (no cancellation):  e[..] = e^{i pm} sum_m i^{m+2} h_m / (m+2)!,
-//    h_m the complete homogeneous symmetric polynomials of the centred points
-//    (|centred point| <= 2D/3), h_m = -e2 h_{m-2} + e3 h_{m-3} (e1 = 0),
-//    truncated after h_12 (remainder < 1e-8).
-//  * otherwise: (f[R,Q] - f[P,R]) / (Q - P) with (P, Q) the pair of vertices
-//    with the largest gap (|Q-P| = D >= 2, so the subtraction loses at most a
-//    factor ~1/D of FP32 precision) and stable first differences.
-__device__ __forceinline__ cf tri_phi_phase(df sa, df sb, df sc, df sm, df k, float al, float be) {
-  float D = fmaxf(fmaxf(fabsf(al), fabsf(be)), fabsf(be - al));
-  if (D < 2.0f) {
-    cf P = cis(df_mul(k, sm));
-    float da = -(al + be) * (1.0f / 3.0f);
-    float db = al + da, dc = be + da;
-    float e2 = -0.5f * (da * da + db * db + dc * dc);
-    float e3 = da * db * dc;
-    float me2 = -e2;
-    float h2 = me2, h3 = e3;
-    float h4 = me2 * h2;
-    float h5 = fmaf(me2, h3, e3 * h2);
-    float h6 = fmaf(me2, h4, e3 * h3);
-    float h7 = fmaf(me2, h5, e3 * h4);
-    float h8 = fmaf(me2, h6, e3 * h5);
-    float h9 = fmaf(me2, h7, e3 * h6);
-    float h10 = fmaf(me2, h8, e3 * h7);
-    float h11 = fmaf(me2, h9, e3 * h8);
-    float h12 = fmaf(me2, h10, e3 * h9);
-    float sre = -0.5f + h2 * (1.0f / 24.0f) - h4 * (1.0f / 720.0f) + h6 * (1.0f / 40320.0f) -
-                h8 * (1.0f / 3628800.0f) + h10 * (1.0f / 479001600.0f) - h12 * (1.0f / 87178291200.0f);
-    float sim = h3 * (1.0f / 120.0f) - h5 * (1.0f / 5040.0f) + h7 * (1.0f / 362880.0f) -
-                h9 * (1.0f / 39916800.0f) + h11 * (1.0f / 6227020800.0f);
-    cf r = cmul(P, cf{sre, sim});
-    return {-2.0f * r.re, -2.0f * r.im};
-  }
-  cf Pa = cis(df_mul(k, sa)), Pb = cis(df_mul(k, sb)), Pc = cis(df_mul(k, sc));
-  float gab = al, gac = be, gbc = be - al;
+// tri_series: spread D = max(|al|, |be|, |be-al|) < 2.  Taylor series about the
+//   centroid phase pm = k.m, m = (a+b+c)/3 (no cancellation):
+//     e[pa,pb,pc] = e^{i pm} S,  S = sum_m i^{m+2} h_m / (m+2)!
+//   with h_m the complete homogeneous symmetric polynomials of the centred
+//   points (|centred point| <= 2D/3), h_m = -e2 h_{m-2} + e3 h_{m-3} (e1 = 0),
+//   truncated after h_12 (remainder < 1e-8).  Returns S.
+__device__ __forceinline__ cf tri_series(float al, float be) {
+  const float da = -(al + be) * (1.0f / 3.0f);
+  const float db = al + da, dc = be + da;
+  const float me2 = 0.5f * (da * da + db * db + dc * dc);  // -e2
+  const float e3 = da * db * dc;
+  const float h2 = me2, h3 = e3;
+  const float h4 = me2 * h2;
+  const float h5 = fmaf(me2, h3, e3 * h2);
+  const float h6 = fmaf(me2, h4, e3 * h3);
+  const float h7 = fmaf(me2, h5, e3 * h4);
+  const float h8 = fmaf(me2, h6, e3 * h5);
+  const float h9 = fmaf(me2, h7, e3 * h6);
+  const float h10 = fmaf(me2, h8, e3 * h7);
+  const float h11 = fmaf(me2, h9, e3 * h8);
+  const float h12 = fmaf(me2, h10, e3 * h9);
+  const float sre = -0.5f + h2 * (1.0f / 24.0f) - h4 * (1.0f / 720.0f) + h6 * (1.0f / 40320.0f) -
+                    h8 * (1.0f / 3628800.0f) + h10 * (1.0f / 479001600.0f) - h12 * (1.0f / 87178291200.0f);
+  const float sim = h3 * (1.0f / 120.0f) - h5 * (1.0f / 5040.0f) + h7 * (1.0f / 362880.0f) -
+                    h9 * (1.0f / 39916800.0f) + h11 * (1.0f / 6227020800.0f);
+  return {sre, sim};
+}
+
+// tri_generic: spread D >= 2.  (f[R,Q] - f[P,R]) / (Q - P) with (P, Q) the pair
+// of vertices with the largest gap (|Q-P| = D, so the subtraction loses at
+// most a factor ~1/D of FP32 precision) and stable first differences.
+// Returns e[pa, pb, pc] given the vertex phasors and al = pb-pa, be = pc-pa.
+__device__ __forceinline__ cf tri_generic(cf Pa, cf Pb, cf Pc, float al, float be) {
+  const float gab = al, gac = be, gbc = be - al;
   cf fRQ, fPR;
   float den;
-  if (fabsf(gab) >= fabsf(gac) && fabsf(gab) >= fabsf(gbc)) {
-    // P = a, Q = b, R = c
+  if (fabsf(gab) >= fabsf(gac) && fabsf(gab) >= fabsf(gbc)) {  // P = a, Q = b, R = c
     fRQ = dd1(Pc, Pb, -gbc);
     fPR = dd1(Pa, Pc, gac);
     den = gab;
-  } else if (fabsf(gac) >= fabsf(gbc)) {
-    // P = a, Q = c, R = b
+  } else if (fabsf(gac) >= fabsf(gbc)) {  // P = a, Q = c, R = b
     fRQ = dd1(Pb, Pc, gbc);
     fPR = dd1(Pa, Pb, gab);
     den = gac;
-  } else {
-    // P = b, Q = c, R = a
+  } else {  // P = b, Q = c, R = a
     fRQ = dd1(Pa, Pc, gac);
     fPR = dd1(Pb, Pa, -gab);
     den = gbc;
   }
-  float s = -2.0f * __frcp_rn(den);
+  const float s = __frcp_rn(den);
   return {(fRQ.re - fPR.re) * s, (fRQ.im - fPR.im) * s};
 }
 

@@ -136,7 +136,9 @@ __global__ void prepare_elems_kernel(const PrepObj* objs, const ObjDev* od, floa
     }
     double S[3] = {0.5 * (e1[1] * e2[2] - e1[2] * e2[1]), 0.5 * (e1[2] * e2[0] - e1[0] * e2[2]),
                    0.5 * (e1[0] * e2[1] - e1[1] * e2[0])};
-    dst[0] = make_float4((float)(a[0] - org[0]), (float)(a[1] - org[1]), (float)(a[2] - org[2]), (float)S[0]);
+    // centroid m = a + (e1 + e2)/3 relative to the object origin
+    dst[0] = make_float4((float)(a[0] + (e1[0] + e2[0]) / 3.0 - org[0]), (float)(a[1] + (e1[1] + e2[1]) / 3.0 - org[1]),
+                         (float)(a[2] + (e1[2] + e2[2]) / 3.0 - org[2]), (float)S[0]);
     dst[1] = make_float4((float)e1[0], (float)e1[1], (float)e1[2], (float)S[1]);
     dst[2] = make_float4((float)e2[0], (float)e2[1], (float)e2[2], (float)S[2]);
   } else {
@@ -208,20 +210,42 @@ ff_kernel(KGridDev kg, BatchDev b, float2* __restrict__ J, int scale_sqrt_w) {
       if (active) {
         for (int e = 0; e < cnt; ++e) {
           const float4 q0 = tile[3 * e], q1 = tile[3 * e + 1], q2 = tile[3 * e + 2];
-          const float3 a = make_float3(q0.x, q0.y, q0.z);
+          const float3 m = make_float3(q0.x, q0.y, q0.z);  // centroid, object frame
           const float3 e1 = make_float3(q1.x, q1.y, q1.z);
           const float3 e2 = make_float3(q2.x, q2.y, q2.z);
-          // gamma = khat . S  (times the -2 of Phi = -2 e[0,al,be] folded in tri_phi_phase)
-          const float g = (dh.x * q0.w + dh.y * q1.w + dh.z * q2.w) * inv_norm;
-          const df sa = cdot(dh, dl, a), s1 = cdot(dh, dl, e1), s2 = cdot(dh, dl, e2);
-          const df sb = df_add(sa, s1), sc = df_add(sa, s2);
-          const df sm = df_add(sa, df_scale(df_add(s1, s2), 1.0f / 3.0f));
+          // -2 (khat . S): gamma of the reference times the -2 of Phi = -2 e[..]
+          const float g = -2.0f * (dh.x * q0.w + dh.y * q1.w + dh.z * q2.w) * inv_norm;
+          const df sm = cdot(dh, dl, m);
+          const float s1 = fmaf(dh.x, e1.x, fmaf(dh.y, e1.y, dh.z * e1.z));
+          const float s2 = fmaf(dh.x, e2.x, fmaf(dh.y, e2.y, dh.z * e2.z));
+          const float sp = fmaxf(fmaxf(fabsf(s1), fabsf(s2)), fabsf(s2 - s1));
+          uint32_t gmask = 0;
+          // Branch-free pass: the centroid Taylor series at every radius (the
+          // radii where the spread kmag*sp >= 2 are masked and redone below).
 #pragma unroll
           for (int i = 0; i < R; ++i) {
-            const float al = km[i].hi * s1.hi, be = km[i].hi * s2.hi;
-            const cf v = tri_phi_phase(sa, sb, sc, sm, km[i], al, be);
-            acc_re[i] = fmaf(g, v.re, acc_re[i]);
-            acc_im[i] = fmaf(g, v.im, acc_im[i]);
+            const bool tay = km[i].hi * sp < 2.0f;
+            gmask |= (tay ? 0u : 1u) << i;
+            const float al = tay ? km[i].hi * s1 : 0.f, be = tay ? km[i].hi * s2 : 0.f;
+            const cf v = cmul(cis(df_mul(km[i], sm)), tri_series(al, be));
+            acc_re[i] = tay ? fmaf(g, v.re, acc_re[i]) : acc_re[i];
+            acc_im[i] = tay ? fmaf(g, v.im, acc_im[i]) : acc_im[i];
+          }
+          if (gmask) {
+            // Large-spread radii: vertex phases in double-float
+            // (a = m - (e1 + e2)/3, b = a + e1, c = a + e2).
+            const df d1 = cdot(dh, dl, e1), d2 = cdot(dh, dl, e2);
+            const df sa = df_add(sm, df_div3(df_add(d1, d2)) * -1.0f);
+            const df sb = df_add(sa, d1), sc = df_add(sa, d2);
+#pragma unroll
+            for (int i = 0; i < R; ++i) {
+              if (gmask & (1u << i)) {
+                const cf v = tri_generic(cis(df_mul(km[i], sa)), cis(df_mul(km[i], sb)), cis(df_mul(km[i], sc)),
+                                         km[i].hi * d1.hi, km[i].hi * d2.hi);
+                acc_re[i] = fmaf(g, v.re, acc_re[i]);
+                acc_im[i] = fmaf(g, v.im, acc_im[i]);
+              }
+            }
           }
         }
       }

@@ -62,7 +62,7 @@ struct ObjDev {
 };
 
 // Pools in the kernels' layout, object-local frame, FP32:
-//   triangles: 3 x float4 per element  (a.xyz, S.x) (e1.xyz, S.y) (e2.xyz, S.z)
+//   triangles: 3 x float4 per element  (m.xyz, S.x) (e1.xyz, S.y) (e2.xyz, S.z), m the centroid
 //   disks/Gaussians: 2 x float4        (c.xyz, rho|sigma) (n'.xyz, area|w)
 struct BatchDev {
   int n_obj;
