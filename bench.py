@@ -45,7 +45,7 @@ def parse():
     p.add_argument("--steps", type=int, default=10)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    p.add_argument("--precision", default="auto", choices=["auto", "fp32", "bf16x3"])
+    p.add_argument("--precision", default="auto", choices=["auto", "fp32", "bf16x3", "tf32x3"])
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--cpu-seconds", type=float, default=12.0)
@@ -193,18 +193,7 @@ def run_gb300(args):
     n_tri = meta["n_triangles"]
     Q = kg.num_nodes
     evals_step = n_tri * Q
-    precision = args.precision
-    if precision == "auto":
-        precision = "fp32"
-        try:
-            probe_ws = core.contract_workspace_size(kg, n_obj, "bf16x3")
-            torch.zeros(1, device="cuda")
-            Jt = torch.zeros((n_obj, Q), dtype=torch.complex64, device="cuda")
-            core.contract(kg, Jt, "bf16x3")
-            precision = "bf16x3"
-            del Jt, probe_ws
-        except _lib.PointIntError:
-            precision = "fp32"
+    precision = "tf32x3" if args.precision == "auto" else args.precision
     stream = torch.cuda.current_stream()
     batch = core.ObjectBatch(objs)
     Jw = torch.empty((n_obj, Q), dtype=torch.complex64, device="cuda")
@@ -268,14 +257,27 @@ def run_gb300(args):
             ms.append(a.elapsed_time(b))
         return statistics.median(ms)
 
-    contraction = {"fp32_ms": time_contract("fp32")}
-    V32 = V.clone()
-    if precision == "bf16x3":
-        contraction["bf16x3_ms"] = time_contract("bf16x3")
-        d = torch.sqrt(torch.outer(torch.diagonal(V32), torch.diagonal(V32)).abs())
-        rel = ((V - V32).abs() / torch.maximum(V32.abs(), 1e-3 * d)).max().item()
-        contraction["bf16x3_vs_fp32_max_rel"] = rel
-        contraction["speedup"] = contraction["fp32_ms"] / contraction["bf16x3_ms"]
+    # FP64 reference of the same contraction (cuBLAS DGEMM: a check, not the product path)
+    X = torch.view_as_real(Jw).reshape(n_obj, -1).double()
+    V64 = (X @ X.T) / (8 * np.pi ** 3)
+    d64 = torch.sqrt(torch.outer(torch.diagonal(V64), torch.diagonal(V64)).abs())
+
+    def cond_err(Vx, eps):
+        return ((Vx - V64).abs() / torch.maximum(V64.abs(), eps * d64)).max().item()
+
+    contraction = {"reference": "FP64 contraction of the same J"}
+    for p in ("fp32", "tf32x3", "bf16x3"):
+        try:
+            contraction[p] = {"ms": time_contract(p), "max_rel_err": cond_err(V, 1e-3),
+                              "max_rel_err_floor_1e-2": cond_err(V, 1e-2)}
+        except _lib.PointIntError as exc:
+            contraction[p] = {"error": str(exc)}
+    if "ms" in contraction.get("bf16x3", {}) and "ms" in contraction["fp32"]:
+        contraction["speedup_bf16x3_vs_fp32"] = contraction["fp32"]["ms"] / contraction["bf16x3"]["ms"]
+    if "ms" in contraction.get("tf32x3", {}) and "ms" in contraction["fp32"]:
+        contraction["speedup_tf32x3_vs_fp32"] = contraction["fp32"]["ms"] / contraction["tf32x3"]["ms"]
+    contraction["error_definition"] = "max_ij |dV_ij| / max(|V_ij|, eps sqrt(V_ii V_jj)), eps = 1e-3 (or 1e-2)"
+    del X, V64
 
     sm_clock = clocks.get("sm_mhz") or peaks.get("sm_max_mhz", 2070.0)
     n_sm = torch.cuda.get_device_properties(local).multi_processor_count

@@ -55,8 +55,9 @@ enum { PI_DOF_AFFINE = 0, PI_DOF_TRIANGLE_MESH = 1 };
 enum { PI_VOLUME_ONLY = 1, PI_GRADIENT = 2, PI_HESSIAN = 4, PI_ALL = 7 };
 /* Contraction precision for V = Re(J^H diag(w) J). */
 enum {
-  PI_CONTRACT_FP32 = 0,      /* FP32 SIMT (the plain drop-in)                       */
-  PI_CONTRACT_BF16X3 = 1     /* BF16 hi+lo split on tcgen05 tensor cores, FP32 accum */
+  PI_CONTRACT_FP32 = 0,      /* FP32 SIMT (the plain drop-in)                                    */
+  PI_CONTRACT_BF16X3 = 1,    /* BF16 hi+lo split on tcgen05 tensor cores, FP32 accumulation      */
+  PI_CONTRACT_TF32X3 = 2     /* TF32 hi+lo split on tcgen05 tensor cores (~21 bits), FP32 accum. */
 };
 
 /* ---- packed element layouts (reference cpp/include/geometry/types.hpp:9-37) */

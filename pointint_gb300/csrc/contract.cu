@@ -107,22 +107,23 @@ syrk_fp32_kernel(const float* __restrict__ X, int n, int64_t K, const float* __r
     *reinterpret_cast<float4*>(&out[(ty * 4 + a) * TB + tx * 4]) = make_float4(acc[a][0], acc[a][1], acc[a][2], acc[a][3]);
 }
 
-// Fixed-order FP64 sum of the split partials, scaled by 1/(8 pi^3), mirrored.
+// Fixed-order FP64 sum of the split partials, scaled by 1/(8 pi^3), mirrored;
+// one thread per output element of the upper-triangle tiles.
 __global__ void reduce_tiles_kernel(const float* __restrict__ partials, int nsplit, int npairs, int nt, int n,
                                     double* __restrict__ V) {
-  const int p = blockIdx.x;
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (int64_t)npairs * TB * TB) return;
+  const int p = (int)(t / (TB * TB)), e = (int)(t % (TB * TB));
   int bi, bj;
   tile_of(p, nt, &bi, &bj);
-  for (int e = threadIdx.x; e < TB * TB; e += blockDim.x) {
-    const int r = e / TB, c = e % TB;
-    const int i = bi * TB + r, j = bj * TB + c;
-    if (i >= n || j >= n || (bi == bj && r > c)) continue;
-    double s = 0.0;
-    for (int sp = 0; sp < nsplit; ++sp) s += (double)partials[((int64_t)sp * npairs + p) * (TB * TB) + e];
-    s *= INV8PI3;
-    V[(int64_t)i * n + j] = s;
-    V[(int64_t)j * n + i] = s;
-  }
+  const int r = e / TB, c = e % TB;
+  const int i = bi * TB + r, j = bj * TB + c;
+  if (i >= n || j >= n || (bi == bj && r > c)) return;
+  double s = 0.0;
+  for (int sp = 0; sp < nsplit; ++sp) s += (double)partials[((int64_t)sp * npairs + p) * (TB * TB) + e];
+  s *= INV8PI3;
+  V[(int64_t)i * n + j] = s;
+  V[(int64_t)j * n + i] = s;
 }
 
 struct SyrkPlan { int nt, npairs, nsplit; int64_t K, kchunk; };
@@ -165,7 +166,9 @@ int launch_contract_fp32(const pi_kgrid_impl* kg, const float2* Jw, int n, doubl
                                         kg->all_positive ? nullptr : kg->dev.sign, p.nt, p.kchunk,
                                         static_cast<float*>(ws));
   PI_LAUNCHED("syrk_fp32_kernel");
-  reduce_tiles_kernel<<<p.npairs, 256, 0, s>>>(static_cast<const float*>(ws), p.nsplit, p.npairs, p.nt, n, V);
+  const int64_t total = (int64_t)p.npairs * TB * TB;
+  reduce_tiles_kernel<<<(unsigned)((total + 255) / 256), 256, 0, s>>>(static_cast<const float*>(ws), p.nsplit,
+                                                                      p.npairs, p.nt, n, V);
   PI_LAUNCHED("reduce_tiles_kernel");
   return PI_OK;
 }

@@ -1,4 +1,5 @@
-// Volume contraction on tcgen05 tensor cores: BF16 hi+lo split, FP32 accumulation.
+// Volume contraction on tcgen05 tensor cores: hi+lo split operands (BF16 or
+// TF32), FP32 accumulation.
 //
 // V = X X^T with X = [Re sqrt|w| J ; Im sqrt|w| J] (n x 2Q, the FP32 layout the
 // form-factor kernel writes).  Each FP32 operand value x is split into
@@ -31,20 +32,30 @@ namespace pi {
 namespace {
 
 constexpr int TC_M = 128;                       // tile edge (objects)
-constexpr int TC_KC = 64;                       // K elements per stage = one 128-byte bf16 row
 constexpr int TC_STAGES = 3;
 constexpr int TC_PWARPS = 8;                    // producer warps
 constexpr int TC_THREADS = (TC_PWARPS + 1) * 32;
-constexpr int BLK_BYTES = TC_M * TC_KC * 2;     // 16 KB: one bf16 operand block
+constexpr int BLK_BYTES = TC_M * 128;           // 16 KB: one operand block, 128-byte K rows
 constexpr int STAGE_BYTES = 4 * BLK_BYTES;      // A hi, A lo, B hi, B lo
 constexpr int SMEM_BYTES = TC_STAGES * STAGE_BYTES + 1024;  // + alignment slack
 constexpr long long WAIT_CYCLES = 4000000000LL; // ~2 s at 2 GHz
 constexpr double INV8PI3 = 1.0 / (8.0 * 3.14159265358979323846 * 3.14159265358979323846 * 3.14159265358979323846);
 
-// kind::f16 instruction descriptor: D = F32 (bits 4-5 = 1), A = B = BF16
-// (bits 7-9 = 1, 10-12 = 1), both K-major, N >> 3 at bits 17-22, M >> 4 at 24-28.
-constexpr uint32_t IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(TC_M >> 3) << 17) |
-                           ((uint32_t)(TC_M >> 4) << 24);
+// Operand kinds.  A 128-byte K row holds 64 BF16 or 32 TF32 values; each
+// 16-byte chunk of it is produced from EPC FP32 inputs (EPC = 8 or 4).
+enum { KIND_BF16 = 0, KIND_TF32 = 1 };
+template <int KIND> struct Kind;
+template <> struct Kind<KIND_BF16> { static constexpr int EPC = 8; static constexpr uint32_t FMT = 1; };
+template <> struct Kind<KIND_TF32> { static constexpr int EPC = 4; static constexpr uint32_t FMT = 2; };
+
+// Instruction descriptor (kind::f16 / kind::tf32): D = F32 (bits 4-5 = 1), A and
+// B format at bits 7-9 / 10-12 (1 = BF16, 2 = TF32), both K-major, N >> 3 at
+// bits 17-22, M >> 4 at bits 24-28.
+template <int KIND>
+constexpr uint32_t idesc() {
+  return (1u << 4) | (Kind<KIND>::FMT << 7) | (Kind<KIND>::FMT << 10) | ((uint32_t)(TC_M >> 3) << 17) |
+         ((uint32_t)(TC_M >> 4) << 24);
+}
 
 enum { ERR_PRODUCER_WAIT = 1, ERR_MMA_WAIT = 2, ERR_EPILOGUE_WAIT = 3 };
 
@@ -101,12 +112,21 @@ __device__ __forceinline__ uint64_t desc_sw128(uint32_t saddr) {
   return d;
 }
 
-__device__ __forceinline__ void umma_bf16(uint32_t tmem_d, uint64_t a, uint64_t b, uint32_t accumulate) {
-  asm volatile(
-      "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %3, 0;\n\t"
-      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %4, p;\n\t}" ::"r"(tmem_d),
-      "l"(a), "l"(b), "r"(accumulate), "r"(IDESC)
-      : "memory");
+template <int KIND>
+__device__ __forceinline__ void umma(uint32_t tmem_d, uint64_t a, uint64_t b, uint32_t accumulate) {
+  if (KIND == KIND_BF16) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %3, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %4, p;\n\t}" ::"r"(tmem_d),
+        "l"(a), "l"(b), "r"(accumulate), "r"(idesc<KIND_BF16>())
+        : "memory");
+  } else {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %3, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %4, p;\n\t}" ::"r"(tmem_d),
+        "l"(a), "l"(b), "r"(accumulate), "r"(idesc<KIND_TF32>())
+        : "memory");
+  }
 }
 
 __device__ __forceinline__ void umma_commit(uint32_t bar) {
@@ -139,6 +159,24 @@ __device__ __forceinline__ uint32_t pack_bf16(float a, float b) {
   return *reinterpret_cast<uint32_t*>(&v);
 }
 
+__device__ __forceinline__ float to_tf32(float x) {  // round to nearest TF32, kept as an FP32 bit pattern
+  uint32_t r;
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+  return __uint_as_float(r);
+}
+
+// Split 4 consecutive FP32 values into TF32 hi / lo halves (16 B each).
+__device__ __forceinline__ void split4_tf32(const float* x, uint4* hi, uint4* lo) {
+  float h[4], l[4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    h[i] = to_tf32(x[i]);
+    l[i] = to_tf32(x[i] - h[i]);
+  }
+  *hi = make_uint4(__float_as_uint(h[0]), __float_as_uint(h[1]), __float_as_uint(h[2]), __float_as_uint(h[3]));
+  *lo = make_uint4(__float_as_uint(l[0]), __float_as_uint(l[1]), __float_as_uint(l[2]), __float_as_uint(l[3]));
+}
+
 // Split 8 consecutive FP32 values into bf16 hi / lo halves (16 B each).
 __device__ __forceinline__ void split8(const float* x, uint4* hi, uint4* lo) {
   float h[8], l[8];
@@ -151,8 +189,9 @@ __device__ __forceinline__ void split8(const float* x, uint4* hi, uint4* lo) {
   *lo = make_uint4(pack_bf16(l[0], l[1]), pack_bf16(l[2], l[3]), pack_bf16(l[4], l[5]), pack_bf16(l[6], l[7]));
 }
 
+template <int KIND>
 __global__ void __launch_bounds__(TC_THREADS, 1)
-syrk_bf16x3_kernel(const float* __restrict__ X, int n, int64_t K, int nt, int64_t nchunks, int64_t cps,
+syrk_split3_kernel(const float* __restrict__ X, int n, int64_t K, int nt, int64_t nchunks, int64_t cps,
                    float* __restrict__ partials, int* __restrict__ err) {
   extern __shared__ uint8_t smem_raw[];
   __shared__ __align__(8) uint64_t full_bar[TC_STAGES];
@@ -188,31 +227,37 @@ syrk_bf16x3_kernel(const float* __restrict__ X, int n, int64_t K, int nt, int64_
 
   if (warp < TC_PWARPS) {
     // ---------------- producers: FP32 -> bf16 hi/lo, swizzled K-major tiles ----------------
-    const int units = diag ? TC_M * 8 : 2 * TC_M * 8;  // 8-element units per stage
+    constexpr int EPC = Kind<KIND>::EPC;
+    constexpr int KC = 8 * EPC;                          // K elements per stage
+    const int units = diag ? TC_M * 8 : 2 * TC_M * 8;  // 16-byte output chunks per stage
     const bool vec = (K & 3) == 0;
     for (int64_t c = 0; c < nc; ++c) {
       const int s = (int)(c % TC_STAGES);
       const int64_t r = c / TC_STAGES;
       if (r > 0 && !mbar_wait(smem_u32(&empty_bar[s]), (uint32_t)((r - 1) & 1), err, ERR_PRODUCER_WAIT)) break;
       uint8_t* st = smem + s * STAGE_BYTES;
-      const int64_t kbase = (c0 + c) * TC_KC;
+      const int64_t kbase = (c0 + c) * KC;
       for (int u = tid; u < units; u += TC_PWARPS * 32) {
         const int blk = u >= TC_M * 8;
         const int uu = u - blk * TC_M * 8;
         const int row = uu >> 3, ch = uu & 7;
         const int grow = (blk ? bj : bi) * TC_M + row;
-        const int64_t kk = kbase + ch * 8;
-        float x[8];
-        if (vec && grow < n && kk + 8 <= K) {  // 16-byte aligned: K % 4 == 0 and kk % 8 == 0
+        const int64_t kk = kbase + ch * EPC;
+        float x[EPC];
+        if (vec && grow < n && kk + EPC <= K) {  // 16-byte aligned: K % 4 == 0 and kk % 4 == 0
           const float4* src = reinterpret_cast<const float4*>(X + (int64_t)grow * K + kk);
-          const float4 a = __ldg(src), b = __ldg(src + 1);
-          x[0] = a.x; x[1] = a.y; x[2] = a.z; x[3] = a.w; x[4] = b.x; x[5] = b.y; x[6] = b.z; x[7] = b.w;
+#pragma unroll
+          for (int v = 0; v < EPC / 4; ++v) {
+            const float4 a = __ldg(src + v);
+            x[4 * v] = a.x; x[4 * v + 1] = a.y; x[4 * v + 2] = a.z; x[4 * v + 3] = a.w;
+          }
         } else {
 #pragma unroll
-          for (int i = 0; i < 8; ++i) x[i] = (grow < n && kk + i < K) ? X[(int64_t)grow * K + kk + i] : 0.f;
+          for (int i = 0; i < EPC; ++i) x[i] = (grow < n && kk + i < K) ? X[(int64_t)grow * K + kk + i] : 0.f;
         }
         uint4 hi, lo;
-        split8(x, &hi, &lo);
+        if (KIND == KIND_BF16) split8(x, &hi, &lo);
+        else split4_tf32(x, &hi, &lo);
         const uint32_t off = (uint32_t)((row >> 3) * 1024 + (row & 7) * 128 + ((ch ^ (row & 7)) << 4));
         uint8_t* base = st + (blk ? 2 * BLK_BYTES : 0);
         *reinterpret_cast<uint4*>(base + off) = hi;
@@ -234,11 +279,11 @@ syrk_bf16x3_kernel(const float* __restrict__ X, int n, int64_t K, int nt, int64_
       const uint64_t bH = diag ? aH : desc_sw128(st + 2 * BLK_BYTES);
       const uint64_t bL = diag ? aL : desc_sw128(st + 3 * BLK_BYTES);
 #pragma unroll
-      for (int k = 0; k < TC_KC / 16; ++k) {
+      for (int k = 0; k < 4; ++k) {  // one MMA covers 32 bytes of K (16 BF16 / 8 TF32)
         const uint64_t adv = (uint64_t)(k * 32) >> 4;  // +32 bytes along K inside the swizzled row
-        umma_bf16(tmem, aH + adv, bH + adv, (c > 0 || k > 0) ? 1u : 0u);
-        umma_bf16(tmem, aH + adv, bL + adv, 1u);
-        umma_bf16(tmem, aL + adv, bH + adv, 1u);
+        umma<KIND>(tmem, aH + adv, bH + adv, (c > 0 || k > 0) ? 1u : 0u);
+        umma<KIND>(tmem, aH + adv, bL + adv, 1u);
+        umma<KIND>(tmem, aL + adv, bH + adv, 1u);
       }
       umma_commit(smem_u32(&empty_bar[s]));
     }
@@ -274,32 +319,33 @@ syrk_bf16x3_kernel(const float* __restrict__ X, int n, int64_t K, int nt, int64_
   }
 }
 
+// One thread per output element of the upper-triangle tiles.
 __global__ void reduce_tc_tiles_kernel(const float* __restrict__ partials, int nsplit, int npairs, int nt, int n,
                                        const int* __restrict__ err, double* __restrict__ V) {
-  const int p = blockIdx.x;
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (int64_t)npairs * TC_M * TC_M) return;
+  const int p = (int)(t / (TC_M * TC_M)), e = (int)(t % (TC_M * TC_M));
   int bi, bj;
   tile_of(p, nt, &bi, &bj);
-  const bool bad = *err != 0;
-  for (int e = threadIdx.x; e < TC_M * TC_M; e += blockDim.x) {
-    const int r = e / TC_M, c = e % TC_M;
-    const int i = bi * TC_M + r, j = bj * TC_M + c;
-    if (i >= n || j >= n || (bi == bj && r > c)) continue;
-    double s = 0.0;
-    for (int sp = 0; sp < nsplit; ++sp) s += (double)partials[((int64_t)sp * npairs + p) * (TC_M * TC_M) + e];
-    s = bad ? __longlong_as_double(0x7ff8000000000000LL) : s * INV8PI3;
-    V[(int64_t)i * n + j] = s;
-    V[(int64_t)j * n + i] = s;
-  }
+  const int r = e / TC_M, c = e % TC_M;
+  const int i = bi * TC_M + r, j = bj * TC_M + c;
+  if (i >= n || j >= n || (bi == bj && r > c)) return;
+  double s = 0.0;
+  for (int sp = 0; sp < nsplit; ++sp) s += (double)partials[((int64_t)sp * npairs + p) * (TC_M * TC_M) + e];
+  s = (*err != 0) ? __longlong_as_double(0x7ff8000000000000LL) : s * INV8PI3;
+  V[(int64_t)i * n + j] = s;
+  V[(int64_t)j * n + i] = s;
 }
 
 struct TcPlan { int nt, npairs, nsplit; int64_t K, nchunks, cps; };
 
-TcPlan plan_tc(int64_t Q, int n) {
+TcPlan plan_tc(int64_t Q, int n, int kind) {
   TcPlan p;
   p.K = 2 * Q;
   p.nt = (n + TC_M - 1) / TC_M;
   p.npairs = p.nt * (p.nt + 1) / 2;
-  p.nchunks = (p.K + TC_KC - 1) / TC_KC;
+  const int64_t kc = kind == KIND_BF16 ? 64 : 32;
+  p.nchunks = (p.K + kc - 1) / kc;
   int dev = 0, sms = 148;
   if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   int64_t nsplit = std::max<int64_t>(1, sms / p.npairs);
@@ -311,32 +357,40 @@ TcPlan plan_tc(int64_t Q, int n) {
 
 }  // namespace
 
-size_t contract_tc_ws_bytes(int64_t Q, int n) {
+size_t contract_tc_ws_bytes(int64_t Q, int n, int kind) {
   if (n <= 0 || Q <= 0) return 0;
-  TcPlan p = plan_tc(Q, n);
+  TcPlan p = plan_tc(Q, n, kind);
   return 256 + (size_t)p.nsplit * p.npairs * TC_M * TC_M * sizeof(float);
 }
 
-int launch_contract_tc(const pi_kgrid_impl* kg, const float2* Jw, int n, double* V, void* ws, size_t ws_bytes,
-                       cudaStream_t s) {
+int launch_contract_tc(const pi_kgrid_impl* kg, const float2* Jw, int n, int kind, double* V, void* ws,
+                       size_t ws_bytes, cudaStream_t s) {
   if (n <= 0) return PI_OK;
-  TcPlan p = plan_tc(kg->Q, n);
+  TcPlan p = plan_tc(kg->Q, n, kind);
   const size_t need = 256 + (size_t)p.nsplit * p.npairs * TC_M * TC_M * sizeof(float);
   if (ws_bytes < need || !ws) return fail(PI_ERR_WORKSPACE_TOO_SMALL, "tensor-core contraction workspace too small");
   if ((reinterpret_cast<uintptr_t>(Jw) & 15) != 0) return fail(PI_ERR_INVALID_ARGUMENT, "J must be 16-byte aligned");
-  static bool attr_set = false;
-  if (!attr_set) {
-    PI_CUDA(cudaFuncSetAttribute(syrk_bf16x3_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
-    attr_set = true;
+  static bool attr_set[2] = {false, false};
+  if (!attr_set[kind]) {
+    if (kind == KIND_BF16)
+      PI_CUDA(cudaFuncSetAttribute(syrk_split3_kernel<KIND_BF16>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
+    else
+      PI_CUDA(cudaFuncSetAttribute(syrk_split3_kernel<KIND_TF32>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
+    attr_set[kind] = true;
   }
   int* err = static_cast<int*>(ws);
   float* partials = reinterpret_cast<float*>(static_cast<unsigned char*>(ws) + 256);
   PI_CUDA(cudaMemsetAsync(err, 0, sizeof(int), s));
   dim3 grid((unsigned)p.npairs, (unsigned)p.nsplit);
-  syrk_bf16x3_kernel<<<grid, TC_THREADS, SMEM_BYTES, s>>>(reinterpret_cast<const float*>(Jw), n, p.K, p.nt,
-                                                         p.nchunks, p.cps, partials, err);
-  PI_LAUNCHED("syrk_bf16x3_kernel");
-  reduce_tc_tiles_kernel<<<p.npairs, 256, 0, s>>>(partials, p.nsplit, p.npairs, p.nt, n, err, V);
+  if (kind == KIND_BF16)
+    syrk_split3_kernel<KIND_BF16><<<grid, TC_THREADS, SMEM_BYTES, s>>>(reinterpret_cast<const float*>(Jw), n, p.K,
+                                                                      p.nt, p.nchunks, p.cps, partials, err);
+  else
+    syrk_split3_kernel<KIND_TF32><<<grid, TC_THREADS, SMEM_BYTES, s>>>(reinterpret_cast<const float*>(Jw), n, p.K,
+                                                                      p.nt, p.nchunks, p.cps, partials, err);
+  PI_LAUNCHED("syrk_split3_kernel");
+  const int64_t total = (int64_t)p.npairs * TC_M * TC_M;
+  reduce_tc_tiles_kernel<<<(unsigned)((total + 255) / 256), 256, 0, s>>>(partials, p.nsplit, p.npairs, p.nt, n, err, V);
   PI_LAUNCHED("reduce_tc_tiles_kernel");
   return PI_OK;
 }

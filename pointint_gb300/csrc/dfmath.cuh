@@ -48,6 +48,13 @@ __device__ __forceinline__ df operator*(df a, float s) {  // a * s for s = +-1 o
   return {a.hi * s, a.lo * s};
 }
 
+// a * b as an unnormalised pair (hi, lo) -- enough for reduce_2pi, which
+// treats hi and lo separately.
+__device__ __forceinline__ df df_mul_un(df a, df b) {
+  const float p = a.hi * b.hi;
+  return {p, fmaf(a.hi, b.lo, fmaf(a.lo, b.hi, fmaf(a.hi, b.hi, -p)))};
+}
+
 __device__ __forceinline__ df df_scale(df a, float s) {  // a * s, s exact
   df p = two_prod(a.hi, s);
   return quick_two_sum(p.hi, fmaf(a.lo, s, p.lo));
@@ -64,11 +71,11 @@ __device__ __forceinline__ df cdot(float3 dh, float3 dl, float3 x) {
 
 // 2 pi = 6.28318530717958647692528676655900576839...
 //   TWO_PI_A = FP32(2 pi)                      = 6.28318548202514648437500
-//   TWO_PI_B = FP32(2 pi - TWO_PI_A)           = -1.7484556025237907e-07
+//   TWO_PI_B = FP32(2 pi - TWO_PI_A)           = -1.7484555314695172e-07
 // |2 pi - A - B| < 1e-14, so n * (2 pi - A - B) < 1e-9 for |n| < 1e5.
 #define PI_TWO_PI_A 6.28318548202514648437500f
-#define PI_TWO_PI_B (-1.7484556025237907e-07f)
-#define PI_INV_TWO_PI 0.15915494309189533577f
+#define PI_TWO_PI_B (-1.7484555314695172e-07f)
+#define PI_INV_TWO_PI 0.15915493667125702f
 
 // Reduces a double-float phase to r in about [-pi, pi] with absolute error
 // ~3e-7 rad for |x| < 2^17; fmaf(-n, A, x) is exact because the result has at
@@ -152,6 +159,52 @@ __device__ __forceinline__ cf tri_series(float al, float be) {
   const float sim = h3 * (1.0f / 120.0f) - h5 * (1.0f / 5040.0f) + h7 * (1.0f / 362880.0f) -
                     h9 * (1.0f / 39916800.0f) + h11 * (1.0f / 6227020800.0f);
   return {sre, sim};
+}
+
+// The same series as a polynomial in the radius k for a fixed element and
+// direction: with the centred direction dots d (so the centred phases are k d),
+// -e2 = k^2 mu and e3 = k^3 nu, hence h_m = k^m H_m with H_m = mu H_{m-2} +
+// nu H_{m-3}, and
+//   Re S = sum_j a_j u^j (u = k^2),   Im S = k^3 sum_j b_j u^j.
+// tri_series_coeffs returns g * a_0..a_6 and g * b_0..b_4 so that one radius
+// costs two Horner chains.
+struct TriPoly { float a[7], b[5]; };
+
+__device__ __forceinline__ TriPoly tri_series_coeffs(float s1, float s2, float g) {
+  const float da = -(s1 + s2) * (1.0f / 3.0f);
+  const float db = s1 + da, dc = s2 + da;
+  const float mu = 0.5f * (da * da + db * db + dc * dc);
+  const float nu = da * db * dc;
+  const float H2 = mu, H3 = nu, H4 = mu * H2;
+  const float H5 = fmaf(mu, H3, nu * H2);
+  const float H6 = fmaf(mu, H4, nu * H3);
+  const float H7 = fmaf(mu, H5, nu * H4);
+  const float H8 = fmaf(mu, H6, nu * H5);
+  const float H9 = fmaf(mu, H7, nu * H6);
+  const float H10 = fmaf(mu, H8, nu * H7);
+  const float H11 = fmaf(mu, H9, nu * H8);
+  const float H12 = fmaf(mu, H10, nu * H9);
+  TriPoly t;
+  t.a[0] = -0.5f * g;
+  t.a[1] = H2 * (g / 24.0f);
+  t.a[2] = -H4 * (g / 720.0f);
+  t.a[3] = H6 * (g / 40320.0f);
+  t.a[4] = -H8 * (g / 3628800.0f);
+  t.a[5] = H10 * (g / 479001600.0f);
+  t.a[6] = -H12 * (g / 87178291200.0f);
+  t.b[0] = H3 * (g / 120.0f);
+  t.b[1] = -H5 * (g / 5040.0f);
+  t.b[2] = H7 * (g / 362880.0f);
+  t.b[3] = -H9 * (g / 39916800.0f);
+  t.b[4] = H11 * (g / 6227020800.0f);
+  return t;
+}
+
+__device__ __forceinline__ cf tri_series_eval(const TriPoly& t, float k) {
+  const float u = k * k;
+  const float re = fmaf(u, fmaf(u, fmaf(u, fmaf(u, fmaf(u, fmaf(u, t.a[6], t.a[5]), t.a[4]), t.a[3]), t.a[2]), t.a[1]), t.a[0]);
+  const float im = (k * u) * fmaf(u, fmaf(u, fmaf(u, fmaf(u, t.b[4], t.b[3]), t.b[2]), t.b[1]), t.b[0]);
+  return {re, im};
 }
 
 // tri_generic: spread D >= 2.  (f[R,Q] - f[P,R]) / (Q - P) with (P, Q) the pair

@@ -20,6 +20,7 @@
 #include <algorithm>
 #include "pi_internal.h"
 #include "dfmath.cuh"
+#include "bessel.cuh"
 
 namespace pi {
 
@@ -156,16 +157,6 @@ constexpr int FF_THREADS = 256;
 constexpr int FF_WARPS = FF_THREADS / 32;
 constexpr int FF_TILE = 256;  // elements staged per shared-memory tile
 
-// J1(x)/x for the disk's 2 area J1(rho r)/(rho r)
-// (reference Disk_J1_over_x, cpp/src/element_functions.cpp:100-109).
-__device__ __forceinline__ float j1_over_x(float x) {
-  if (x < 1e-3f) {
-    float x2 = x * x;
-    return fmaf(x2, fmaf(x2, 1.0f / 384.0f, -1.0f / 16.0f), 0.5f);
-  }
-  return j1f(x) / x;
-}
-
 template <int R>
 __global__ void __launch_bounds__(FF_THREADS, 2)
 ff_kernel(KGridDev kg, BatchDev b, float2* __restrict__ J, int scale_sqrt_w) {
@@ -186,10 +177,12 @@ ff_kernel(KGridDev kg, BatchDev b, float2* __restrict__ J, int scale_sqrt_w) {
     dh = make_float3(h.x, h.y, h.z); dl = make_float3(l.x, l.y, l.z);
     inv_norm = h.w; dnorm = l.w;
   }
+  // radii r = rb + nrb * i: every warp sees small and large k alike, so the
+  // warps of a CTA finish an element tile together.
   df km[R];
 #pragma unroll
   for (int i = 0; i < R; ++i) {
-    int r = rb * R + i;
+    int r = rb + nrb * i;
     float2 k = (active && r < kg.L) ? kg.kmag[r] : make_float2(0.f, 0.f);
     km[i] = df{k.x, k.y};
   }
@@ -219,6 +212,7 @@ ff_kernel(KGridDev kg, BatchDev b, float2* __restrict__ J, int scale_sqrt_w) {
           const float s1 = fmaf(dh.x, e1.x, fmaf(dh.y, e1.y, dh.z * e1.z));
           const float s2 = fmaf(dh.x, e2.x, fmaf(dh.y, e2.y, dh.z * e2.z));
           const float sp = fmaxf(fmaxf(fabsf(s1), fabsf(s2)), fabsf(s2 - s1));
+          const TriPoly tp = tri_series_coeffs(s1, s2, g);
           uint32_t gmask = 0;
           // Branch-free pass: the centroid Taylor series at every radius (the
           // radii where the spread kmag*sp >= 2 are masked and redone below).
@@ -226,10 +220,12 @@ ff_kernel(KGridDev kg, BatchDev b, float2* __restrict__ J, int scale_sqrt_w) {
           for (int i = 0; i < R; ++i) {
             const bool tay = km[i].hi * sp < 2.0f;
             gmask |= (tay ? 0u : 1u) << i;
-            const float al = tay ? km[i].hi * s1 : 0.f, be = tay ? km[i].hi * s2 : 0.f;
-            const cf v = cmul(cis(df_mul(km[i], sm)), tri_series(al, be));
-            acc_re[i] = tay ? fmaf(g, v.re, acc_re[i]) : acc_re[i];
-            acc_im[i] = tay ? fmaf(g, v.im, acc_im[i]) : acc_im[i];
+            const cf S = tri_series_eval(tp, km[i].hi);
+            const cf P = cis(df_mul_un(km[i], sm));
+            const float re = fmaf(P.re, S.re, fmaf(-P.im, S.im, acc_re[i]));
+            const float im = fmaf(P.re, S.im, fmaf(P.im, S.re, acc_im[i]));
+            acc_re[i] = tay ? re : acc_re[i];
+            acc_im[i] = tay ? im : acc_im[i];
           }
           if (gmask) {
             // Large-spread radii: vertex phases in double-float
@@ -275,7 +271,7 @@ ff_kernel(KGridDev kg, BatchDev b, float2* __restrict__ J, int scale_sqrt_w) {
 #pragma unroll
             for (int i = 0; i < R; ++i) {
               const float x = km[i].hi * rr;
-              const float S = (x < 1e-10f) ? 1.0f : 2.0f * j1_over_x(x);
+              const float S = (x < 1e-10f) ? 1.0f : 2.0f * j1x(x);
               const cf P = cis(df_mul(km[i], sc));
               const float m = S * amp;
               acc_re[i] = fmaf(m, P.re, acc_re[i]);
@@ -307,7 +303,7 @@ ff_kernel(KGridDev kg, BatchDev b, float2* __restrict__ J, int scale_sqrt_w) {
   const int64_t Jrow = (int64_t)oi * kg.Q;
 #pragma unroll
   for (int i = 0; i < R; ++i) {
-    const int r = rb * R + i;
+    const int r = rb + nrb * i;
     if (r < kg.L) {
       const int64_t q = (int64_t)r * kg.M + j;
       cf v = cmul(cis(df_mul(km[i], so)), cf{acc_re[i], acc_im[i]});

@@ -106,9 +106,9 @@ int launch_form_factors(const pi_kgrid_impl* kg, const pi_batch_impl* b, int sca
 size_t contract_fp32_ws_bytes(int64_t Q, int n);
 int launch_contract_fp32(const pi_kgrid_impl* kg, const float2* Jw, int n, double* V, void* ws, size_t ws_bytes,
                          cudaStream_t s);
-size_t contract_tc_ws_bytes(int64_t Q, int n);
-int launch_contract_tc(const pi_kgrid_impl* kg, const float2* Jw, int n, double* V, void* ws, size_t ws_bytes,
-                       cudaStream_t s);
+size_t contract_tc_ws_bytes(int64_t Q, int n, int kind);  // kind 0 = BF16 split, 1 = TF32 split
+int launch_contract_tc(const pi_kgrid_impl* kg, const float2* Jw, int n, int kind, double* V, void* ws,
+                       size_t ws_bytes, cudaStream_t s);
 int launch_pair_dot(const pi_kgrid_impl* kg, const float2* Jw, double* d_out, void* ws, cudaStream_t s);
 int launch_to_double2(const float2* J, int64_t n, double* out, cudaStream_t s);
 
