@@ -134,6 +134,9 @@ int pi_batch_create(const pi_object* objs, int n_objects, int on_device, pi_stre
 /* Replace the DoF vector of object `index` (device pointer, same length) and
  * re-transform it, stream-ordered. */
 int pi_batch_set_dofs(pi_batch b, int index, const double* d_dofs, pi_stream stream);
+/* Replace every object's DoF vector at once: d_dofs holds the vectors
+ * concatenated in object order (device doubles); re-transforms all objects. */
+int pi_batch_set_all_dofs(pi_batch b, const double* d_dofs, pi_stream stream);
 /* Re-run the DoF transform of every object from the batch's current DoF
  * vectors (stream-ordered). */
 int pi_batch_prepare(pi_batch b, pi_stream stream);
@@ -158,6 +161,35 @@ int pi_contract_workspace_size(pi_kgrid kg, int n_objects, int precision, size_t
 int pi_contract(pi_kgrid kg, const void* d_Jw, int n_objects, int precision, double* d_V, void* d_ws,
                 size_t ws_bytes, pi_stream stream);
 
+/* Replace the packed elements of object `index` (device pointer, same count and
+ * layout) and re-transform it; used by optimisation loops that move elements. */
+int pi_batch_set_elements(pi_batch b, int index, const void* d_elems, pi_stream stream);
+/* Where object `index` sits in the batch's element pool of its type and in the
+ * concatenated DoF-gradient vector. */
+int pi_batch_layout(pi_batch b, int index, int64_t* pool_offset, int64_t* n_elems, int64_t* dof_offset);
+
+/* ---- adjoint: gradients of L = sum_ij C_ij V_ij ------------------------------- */
+/* The cotangent of object i is B_i = sum_j W_ij A_j (host W, n x n doubles):
+ * pass W = C + C^T for a loss L = sum_ij C_ij V_ij, or W with a single column
+ * of ones (W_ij = [j == j0]) for the reference's per-pair gradients
+ * dV_{i j0}/dtheta_i (grad_matrix[i][j0], cpp/include/compute_intersection_volume_multi_object.hpp:21-26).
+ * d_Jw is the sqrt(|w|)-scaled J of the batch (pi_form_factors with
+ * scale_sqrt_w = 1).  Replaces K4-K6, K8, K10, K15
+ * (cpp/src/dof/cuda/affine_dof_cuda.cu:254-576, 693-849; cpp/src/dof/cuda/triangle_mesh_dof_cuda.cu:147-310;
+ *  cpp/src/compute_intersection_volume.cu:60-101; cpp/src/compute_intersection_volume_multi_object.cu:124-176)
+ * without materialising dA/dtheta per k-node. */
+int pi_adjoint_workspace_size(pi_kgrid kg, pi_batch b, size_t* bytes);
+/* Per-element gradients (device float outputs in pool order, either may be NULL):
+ *   triangles: 9 per element = dL/dv0, dL/dv1, dL/dv2 (world-frame vertex positions);
+ *   disks / Gaussians: 12 per element = dL/dc (3), dL/dn' (3, n' = A n), dL/dM (6: xx xy xz yy yz zz, M = A A^T). */
+int pi_element_gradients(pi_kgrid kg, pi_batch b, const void* d_Jw, const double* W, float* d_tri_grad,
+                         float* d_surf_grad, void* d_ws, size_t ws_bytes, pi_stream stream);
+/* DoF gradients of every object concatenated in object order (device doubles):
+ * 12 per AffineDoF object ([t, A row-major], affine_dof.cpp:172-322 chain rule),
+ * 3V per TriangleMeshDoF object (triangle_mesh_dof.cpp:76-143). */
+int pi_dof_gradients(pi_kgrid kg, pi_batch b, const void* d_Jw, const double* W, double* d_grad, void* d_ws,
+                     size_t ws_bytes, pi_stream stream);
+
 /* ---- one-shot host-buffer drop-ins ------------------------------------------ */
 /* compute_intersection_volume_matrix_cuda (cpp/include/compute_intersection_volume_multi_object.hpp:51-59).
  * Host objects and k-grid; V_out: host n x n.  flags: PI_VOLUME_ONLY only in
@@ -167,6 +199,17 @@ int pi_volume_matrix_host(const pi_object* objs, int n_objects, const double* di
 /* compute_intersection_volume_cuda (cpp/include/compute_intersection_volume.hpp:48-59), volume. */
 int pi_pair_volume_host(const pi_object* o1, const pi_object* o2, const double* dirs, const double* kmag,
                         const double* w, int64_t Q, double* volume);
+/* compute_intersection_volume_cuda with ComputationFlags::GRADIENT
+ * (cpp/include/compute_intersection_volume.hpp:48-59): volume and the DoF
+ * gradients grad_geom1 (o1->n_dofs) / grad_geom2 (o2->n_dofs), host buffers. */
+int pi_pair_volume_grad_host(const pi_object* o1, const pi_object* o2, const double* dirs, const double* kmag,
+                             const double* w, int64_t Q, double* volume, double* grad1, double* grad2);
+/* compute_intersection_volume_matrix_cuda with GRADIENT
+ * (cpp/include/compute_intersection_volume_multi_object.hpp:51-59): V (n x n)
+ * and grad_matrix packed as blocks (i, j) = dV_ij/dtheta_i of n_dofs[i] doubles
+ * at offset n * sum_{m<i} n_dofs[m] + j * n_dofs[i]. */
+int pi_volume_matrix_grad_host(const pi_object* objs, int n_objects, const double* dirs, const double* kmag,
+                               const double* w, int64_t Q, double* V_out, double* grad_out);
 /* CudaComputeAkFunc registry plugin (cpp/include/dof/cuda/dof_cuda_interface.hpp:24-30):
  * host object and k-grid, output d_A_out = Q complex doubles (double2) on the device. */
 int pi_compute_Ak(const pi_object* obj, const double* dirs, const double* kmag, int64_t Q, double* d_A_out,

@@ -69,11 +69,19 @@ SIGNATURES = {
     "pi_batch_create": (I32, [OBJP, I32, I32, P, PP]),
     "pi_batch_set_dofs": (I32, [P, I32, P, P]),
     "pi_batch_prepare": (I32, [P, P]),
+    "pi_batch_set_all_dofs": (I32, [P, P, P]),
     "pi_batch_destroy": (I32, [P]),
     "pi_batch_count": (I32, [P, ctypes.POINTER(I32)]),
     "pi_form_factors": (I32, [P, P, I32, P, P]),
     "pi_contract_workspace_size": (I32, [P, I32, I32, ctypes.POINTER(SZ)]),
     "pi_contract": (I32, [P, P, I32, I32, P, P, SZ, P]),
+    "pi_batch_set_elements": (I32, [P, I32, P, P]),
+    "pi_batch_layout": (I32, [P, I32, ctypes.POINTER(I64), ctypes.POINTER(I64), ctypes.POINTER(I64)]),
+    "pi_adjoint_workspace_size": (I32, [P, P, ctypes.POINTER(SZ)]),
+    "pi_element_gradients": (I32, [P, P, P, P, P, P, P, SZ, P]),
+    "pi_dof_gradients": (I32, [P, P, P, P, P, P, SZ, P]),
+    "pi_pair_volume_grad_host": (I32, [OBJP, OBJP, P, P, P, I64, ctypes.POINTER(D), P, P]),
+    "pi_volume_matrix_grad_host": (I32, [OBJP, I32, P, P, P, I64, P, P]),
     "pi_volume_matrix_host": (I32, [OBJP, I32, P, P, P, I64, I32, I32, P]),
     "pi_pair_volume_host": (I32, [OBJP, OBJP, P, P, P, I64, ctypes.POINTER(D)]),
     "pi_compute_Ak": (I32, [OBJP, P, P, I64, P, I32]),

@@ -64,6 +64,15 @@ class ObjectBatch:
         _lib.check(_lib.lib().pi_batch_set_dofs(self._handle, int(index), ctypes.c_void_p(dofs.data_ptr()),
                                                 _stream(stream)))
 
+    def set_all_dofs(self, dofs: torch.Tensor, stream=None) -> None:
+        """Replace every DoF vector (float64 CUDA tensor, concatenated in object order)."""
+        if not (dofs.is_cuda and dofs.dtype == torch.float64):
+            raise TypeError("dofs must be a float64 CUDA tensor")
+        d = dofs.detach().contiguous()
+        if d.numel() != sum(len(o.dofs) for o in self.objects):
+            raise ValueError("wrong DoF count")
+        _lib.check(_lib.lib().pi_batch_set_all_dofs(self._handle, ctypes.c_void_p(d.data_ptr()), _stream(stream)))
+
     def prepare(self, stream=None) -> None:
         """Re-run the DoF transform of every object (stream-ordered)."""
         _lib.check(_lib.lib().pi_batch_prepare(self._handle, _stream(stream)))
@@ -144,3 +153,167 @@ def volume_matrix_host(kgrid: KGrid, objects: list[SceneObject], precision="fp32
                                                 kgrid.w.ctypes.data, kgrid.num_nodes, _lib.VOLUME_ONLY,
                                                 _precision(precision), V.ctypes.data))
     return V
+
+
+# ----------------------------------------------------------------------------- gradients
+def adjoint_workspace_size(kgrid: KGrid, batch: ObjectBatch) -> int:
+    sz = ctypes.c_size_t(0)
+    _lib.check(_lib.lib().pi_adjoint_workspace_size(kgrid.handle(), batch.handle, ctypes.byref(sz)))
+    return int(sz.value)
+
+
+def _w64(W, n) -> np.ndarray:
+    W = np.ascontiguousarray(np.asarray(W, dtype=np.float64))
+    if W.shape != (n, n):
+        raise ValueError(f"cotangent weights must be {n} x {n}")
+    return W
+
+
+def element_gradients(kgrid: KGrid, batch: ObjectBatch, Jw: torch.Tensor, W, workspace: Workspace | None = None,
+                      stream=None):
+    """Per-element gradients for cotangents B_i = sum_j W_ij A_j (W = C + C^T for
+    L = sum C_ij V_ij).  Returns (tri [n_tri, 9], surf [n_surf, 12]) float32
+    tensors in pool (object) order: triangles dL/dv0,dv1,dv2; surfels dL/dc,
+    dL/dn', dL/dM(6)."""
+    n = len(batch)
+    W = _w64(W, n)
+    n_tri = sum(o.geom.num_elements() for o in batch.objects if o.geom.type == _lib.GEOM_TRIANGLE)
+    n_surf = sum(o.geom.num_elements() for o in batch.objects if o.geom.type != _lib.GEOM_TRIANGLE)
+    tri = torch.empty((max(n_tri, 1), 9), dtype=torch.float32, device="cuda")
+    surf = torch.empty((max(n_surf, 1), 12), dtype=torch.float32, device="cuda")
+    ws = (workspace or _default_ws).get(adjoint_workspace_size(kgrid, batch))
+    _lib.check(_lib.lib().pi_element_gradients(kgrid.handle(), batch.handle, ctypes.c_void_p(Jw.data_ptr()),
+                                               W.ctypes.data, ctypes.c_void_p(tri.data_ptr()),
+                                               ctypes.c_void_p(surf.data_ptr()), ctypes.c_void_p(ws.data_ptr()),
+                                               ctypes.c_size_t(ws.numel()), _stream(stream)))
+    return tri[:n_tri], surf[:n_surf]
+
+
+def dof_gradients(kgrid: KGrid, batch: ObjectBatch, Jw: torch.Tensor, W, workspace: Workspace | None = None,
+                  stream=None) -> torch.Tensor:
+    """DoF gradients of every object, concatenated in object order (float64)."""
+    n = len(batch)
+    W = _w64(W, n)
+    nd = sum(len(o.dofs) for o in batch.objects)
+    g = torch.empty(max(nd, 1), dtype=torch.float64, device="cuda")
+    ws = (workspace or _default_ws).get(adjoint_workspace_size(kgrid, batch))
+    _lib.check(_lib.lib().pi_dof_gradients(kgrid.handle(), batch.handle, ctypes.c_void_p(Jw.data_ptr()), W.ctypes.data,
+                                           ctypes.c_void_p(g.data_ptr()), ctypes.c_void_p(ws.data_ptr()),
+                                           ctypes.c_size_t(ws.numel()), _stream(stream)))
+    return g[:nd]
+
+
+def pair_volume_grad_host(kgrid: KGrid, o1: SceneObject, o2: SceneObject):
+    """Reference compute_intersection_volume_cuda(..., GRADIENT): (volume, grad1, grad2)."""
+    c1, c2 = o1.as_c(), o2.as_c()
+    v = ctypes.c_double(0.0)
+    g1, g2 = np.zeros(len(o1.dofs)), np.zeros(len(o2.dofs))
+    _lib.check(_lib.lib().pi_pair_volume_grad_host(ctypes.byref(c1), ctypes.byref(c2), kgrid.dirs.ctypes.data,
+                                                   kgrid.kmag.ctypes.data, kgrid.w.ctypes.data, kgrid.num_nodes,
+                                                   ctypes.byref(v), g1.ctypes.data, g2.ctypes.data))
+    return float(v.value), g1, g2
+
+
+def volume_matrix_grad_host(kgrid: KGrid, objects: list[SceneObject]):
+    """Reference compute_intersection_volume_matrix_cuda(..., GRADIENT): (V, grad)
+    with grad[i][j] = dV_ij/dtheta_i."""
+    n = len(objects)
+    nd = [len(o.dofs) for o in objects]
+    V = np.zeros((n, n))
+    g = np.zeros(max(1, n * sum(nd)))
+    arr = (_lib.PiObject * n)(*[o.as_c() for o in objects])
+    _lib.check(_lib.lib().pi_volume_matrix_grad_host(arr, n, kgrid.dirs.ctypes.data, kgrid.kmag.ctypes.data,
+                                                     kgrid.w.ctypes.data, kgrid.num_nodes, V.ctypes.data,
+                                                     g.ctypes.data))
+    grad, off = [], 0
+    for i in range(n):
+        grad.append([g[off + j * nd[i]: off + (j + 1) * nd[i]].copy() for j in range(n)])
+        off += n * nd[i]
+    return V, grad
+
+
+class _DofVolumeFn(torch.autograd.Function):
+    """V(theta) for all DoFs theta (concatenated), backward through the adjoint."""
+
+    @staticmethod
+    def forward(ctx, scene, dofs):
+        scene.batch.set_all_dofs(dofs)
+        Jw = form_factors(scene.kgrid, scene.batch, True)
+        V = contract(scene.kgrid, Jw, scene.precision)
+        ctx.scene, ctx.Jw = scene, Jw
+        return V
+
+    @staticmethod
+    def backward(ctx, gV):
+        G = gV.detach().double().cpu().numpy()
+        g = dof_gradients(ctx.scene.kgrid, ctx.scene.batch, ctx.Jw, G + G.T)
+        return None, g
+
+
+class _SurfelVolumeFn(torch.autograd.Function):
+    """V(c, n) for surfel-only scenes; gradients w.r.t. every disk / Gaussian
+    centre and (unnormalised) normal through the adjoint."""
+
+    @staticmethod
+    def forward(ctx, scene, c, n):
+        scene.set_surfels(c, n)
+        Jw = form_factors(scene.kgrid, scene.batch, True)
+        V = contract(scene.kgrid, Jw, scene.precision)
+        ctx.scene, ctx.Jw = scene, Jw
+        return V
+
+    @staticmethod
+    def backward(ctx, gV):
+        G = gV.detach().double().cpu().numpy()
+        _, surf = element_gradients(ctx.scene.kgrid, ctx.scene.batch, ctx.Jw, G + G.T)
+        return None, surf[:, 0:3].double(), surf[:, 3:6].double()
+
+
+class Scene:
+    """Device-resident objects + k-grid with differentiable volume matrices.
+
+        scene = Scene(kgrid, objects)
+        V = scene.volume_matrix_of_dofs(theta)        # theta: concatenated DoFs, requires_grad
+        V = scene.volume_matrix_of_surfels(c, n)       # surfel scenes: centres / normals
+        V.sum().backward()
+    """
+
+    def __init__(self, kgrid: KGrid, objects: list[SceneObject], precision="fp32"):
+        self.kgrid = kgrid
+        self.objects = list(objects)
+        self.batch = ObjectBatch(self.objects)
+        self.precision = precision
+        self.counts = [o.geom.num_elements() for o in self.objects]
+        self._packed = None
+
+    def dofs(self) -> torch.Tensor:
+        return torch.tensor(np.concatenate([o.dofs for o in self.objects]), dtype=torch.float64, device="cuda")
+
+    def volume_matrix_of_dofs(self, dofs: torch.Tensor) -> torch.Tensor:
+        return _DofVolumeFn.apply(self, dofs)
+
+    def surfel_params(self):
+        """Current (c, n) of every surfel, concatenated in object order (float64 CUDA)."""
+        e = np.concatenate([o.geom.elems for o in self.objects])
+        c = torch.tensor(np.stack([e["c"][:, i] for i in range(3)], 1), device="cuda")
+        n = torch.tensor(np.stack([e["n"][:, i] for i in range(3)], 1), device="cuda")
+        return c, n
+
+    def set_surfels(self, c: torch.Tensor, n: torch.Tensor) -> None:
+        if any(o.geom.type == _lib.GEOM_TRIANGLE for o in self.objects):
+            raise TypeError("surfel parameters apply to disk / Gaussian scenes only")
+        if self._packed is None:
+            e = np.concatenate([o.geom.elems for o in self.objects])
+            self._packed = torch.tensor(e.view(np.float64).reshape(-1, 8), device="cuda")
+        self._packed[:, 0:3] = c.detach()
+        self._packed[:, 3:6] = n.detach()
+        off = 0
+        s = _stream(None)
+        for i, cnt in enumerate(self.counts):
+            _lib.check(_lib.lib().pi_batch_set_elements(self.batch.handle, i,
+                                                        ctypes.c_void_p(self._packed[off].data_ptr()) if cnt else None,
+                                                        s))
+            off += cnt
+
+    def volume_matrix_of_surfels(self, c: torch.Tensor, n: torch.Tensor) -> torch.Tensor:
+        return _SurfelVolumeFn.apply(self, c, n)

@@ -66,6 +66,54 @@ struct DevBuf {
 };
 
 struct KGridGuard { pi_kgrid k = nullptr; ~KGridGuard() { if (k) pi_kgrid_destroy(k); } };
+
+// Vertex -> (triangle, slot) adjacency of every TriangleMeshDoF object, for
+// the deterministic per-vertex gather of the adjoint.  Device-resident
+// elements are read back once.
+int build_vertex_csr(pi_batch_impl* b, const pi_object* objs, int on_device, cudaStream_t s) {
+  int64_t nv = 0, goff = 0;
+  std::vector<int64_t> voff(b->n_obj, -1), gofs(b->n_obj);
+  for (int i = 0; i < b->n_obj; ++i) {
+    gofs[i] = goff;
+    goff += b->info[i].n_dofs;
+    if (b->info[i].dof_type == PI_DOF_TRIANGLE_MESH) { voff[i] = nv; nv += b->info[i].n_dofs / 3; }
+  }
+  b->n_mesh_verts = nv;
+  if (nv == 0) return PI_OK;
+  std::vector<std::vector<int64_t>> adj(nv);
+  for (int i = 0; i < b->n_obj; ++i) {
+    if (voff[i] < 0) continue;
+    const HostObjInfo& in = b->info[i];
+    std::vector<pi_tri_packed> tmp;
+    const pi_tri_packed* T = static_cast<const pi_tri_packed*>(objs[i].elems);
+    if (on_device) {
+      tmp.resize(in.n_elems);
+      PI_CUDA(cudaMemcpyAsync(tmp.data(), objs[i].elems, in.n_elems * sizeof(pi_tri_packed), cudaMemcpyDeviceToHost, s));
+      PI_CUDA(cudaStreamSynchronize(s));
+      T = tmp.data();
+    }
+    const int64_t nvi = in.n_dofs / 3;
+    for (int64_t f = 0; f < in.n_elems; ++f) {
+      const int32_t v[3] = {T[f].vid0, T[f].vid1, T[f].vid2};
+      if (v[0] < 0 || v[1] < 0 || v[2] < 0 || v[0] >= nvi || v[1] >= nvi || v[2] >= nvi) continue;
+      for (int sl = 0; sl < 3; ++sl) adj[voff[i] + v[sl]].push_back((in.pool_off + f) * 3 + sl);
+    }
+  }
+  std::vector<int64_t> row(nv + 1, 0), ent, vmap(nv);
+  for (int64_t v = 0; v < nv; ++v) row[v + 1] = row[v] + (int64_t)adj[v].size();
+  ent.reserve(row[nv]);
+  for (auto& a : adj) ent.insert(ent.end(), a.begin(), a.end());
+  for (int i = 0; i < b->n_obj; ++i)
+    if (voff[i] >= 0)
+      for (int64_t v = 0; v < b->info[i].n_dofs / 3; ++v) vmap[voff[i] + v] = gofs[i] + 3 * v;
+  PI_CUDA(cudaMalloc((void**)&b->d_vrow, row.size() * sizeof(int64_t)));
+  PI_CUDA(cudaMalloc((void**)&b->d_vent, std::max<size_t>(ent.size(), 1) * sizeof(int64_t)));
+  PI_CUDA(cudaMalloc((void**)&b->d_vmap, vmap.size() * sizeof(int64_t)));
+  PI_CUDA(cudaMemcpy(b->d_vrow, row.data(), row.size() * sizeof(int64_t), cudaMemcpyHostToDevice));
+  if (!ent.empty()) PI_CUDA(cudaMemcpy(b->d_vent, ent.data(), ent.size() * sizeof(int64_t), cudaMemcpyHostToDevice));
+  PI_CUDA(cudaMemcpy(b->d_vmap, vmap.data(), vmap.size() * sizeof(int64_t), cudaMemcpyHostToDevice));
+  return PI_OK;
+}
 struct BatchGuard { pi_batch b = nullptr; ~BatchGuard() { if (b) pi_batch_destroy(b); } };
 
 }  // namespace
@@ -193,7 +241,7 @@ int pi_batch_create(const pi_object* objs, int n, int on_device, pi_stream strea
                    [&](int a, int c) { return b->info[a].n_elems > b->info[c].n_elems; });
   auto cleanup = [&]() {
     cudaFree(b->d_src); cudaFree(b->d_dofs); cudaFree(b->d_tri_pool); cudaFree(b->d_surf_pool);
-    cudaFree(b->d_objs); cudaFree(b->d_order);
+    cudaFree(b->d_objs); cudaFree(b->d_order); cudaFree(b->d_vrow); cudaFree(b->d_vent); cudaFree(b->d_vmap);
   };
   cudaError_t e = cudaSuccess;
   if (e == cudaSuccess) e = cudaMalloc(&b->d_src, std::max<size_t>(src_bytes, 16));
@@ -227,6 +275,8 @@ int pi_batch_create(const pi_object* objs, int n, int on_device, pi_stream strea
   if (e == cudaSuccess)
     e = cudaMemcpyAsync(b->d_order, b->order.data(), n * sizeof(int32_t), cudaMemcpyHostToDevice, s);
   if (e != cudaSuccess) { cleanup(); return cuda_fail(e, "pi_batch_create upload"); }
+  int rc0 = build_vertex_csr(b.get(), objs, on_device, s);
+  if (rc0) { cleanup(); return rc0; }
   int rc = launch_prepare(b.get(), -1, s);
   if (rc) { cleanup(); return rc; }
   *out = b.release();
@@ -242,6 +292,14 @@ int pi_batch_set_dofs(pi_batch b, int index, const double* d_dofs, pi_stream str
   return launch_prepare(b, index, s);
 }
 
+int pi_batch_set_all_dofs(pi_batch b, const double* d_dofs, pi_stream stream) {
+  if (!b || (!d_dofs && b->n_obj > 0)) return fail(PI_ERR_INVALID_ARGUMENT, "pi_batch_set_all_dofs: bad arguments");
+  cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  const int64_t nd = dof_gradient_size(b);
+  if (nd) PI_CUDA(cudaMemcpyAsync(b->d_dofs, d_dofs, nd * sizeof(double), cudaMemcpyDeviceToDevice, s));
+  return launch_prepare(b, -1, s);
+}
+
 int pi_batch_prepare(pi_batch b, pi_stream stream) {
   if (!b) return fail(PI_ERR_INVALID_ARGUMENT, "pi_batch_prepare: null batch");
   return launch_prepare(b, -1, reinterpret_cast<cudaStream_t>(stream));
@@ -250,7 +308,7 @@ int pi_batch_prepare(pi_batch b, pi_stream stream) {
 int pi_batch_destroy(pi_batch b) {
   if (!b) return PI_OK;
   cudaFree(b->d_src); cudaFree(b->d_dofs); cudaFree(b->d_tri_pool); cudaFree(b->d_surf_pool);
-  cudaFree(b->d_objs); cudaFree(b->d_order);
+  cudaFree(b->d_objs); cudaFree(b->d_order); cudaFree(b->d_vrow); cudaFree(b->d_vent); cudaFree(b->d_vmap);
   delete b;
   return PI_OK;
 }
@@ -287,6 +345,58 @@ int pi_contract(pi_kgrid kg, const void* d_Jw, int n, int precision, double* d_V
     return launch_contract_tc(kg, J, n, precision == PI_CONTRACT_BF16X3 ? 0 : 1, d_V, d_ws, ws_bytes, s);
   }
   return fail(PI_ERR_INVALID_ARGUMENT, "unknown contraction precision");
+}
+
+int pi_batch_set_elements(pi_batch b, int index, const void* d_elems, pi_stream stream) {
+  if (!b || index < 0 || index >= b->n_obj || (!d_elems && b->info[index].n_elems > 0))
+    return fail(PI_ERR_INVALID_ARGUMENT, "pi_batch_set_elements: bad arguments");
+  cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  const HostObjInfo& in = b->info[index];
+  if (in.n_elems)
+    PI_CUDA(cudaMemcpyAsync(static_cast<unsigned char*>(b->d_src) + in.src_off, d_elems,
+                            in.n_elems * elem_bytes(in.geom_type), cudaMemcpyDeviceToDevice, s));
+  return launch_prepare(b, index, s);
+}
+
+int pi_batch_layout(pi_batch b, int index, int64_t* pool_offset, int64_t* n_elems, int64_t* dof_offset) {
+  if (!b || index < 0 || index >= b->n_obj) return fail(PI_ERR_INVALID_ARGUMENT, "pi_batch_layout: bad arguments");
+  const HostObjInfo& in = b->info[index];
+  int64_t dof = 0;
+  for (int i = 0; i < index; ++i) dof += b->info[i].n_dofs;
+  if (pool_offset) *pool_offset = in.pool_off;
+  if (n_elems) *n_elems = in.n_elems;
+  if (dof_offset) *dof_offset = dof;
+  return PI_OK;
+}
+
+int pi_adjoint_workspace_size(pi_kgrid kg, pi_batch b, size_t* bytes) {
+  if (!kg || !b || !bytes) return fail(PI_ERR_INVALID_ARGUMENT, "pi_adjoint_workspace_size: bad arguments");
+  *bytes = adjoint_ws_bytes(kg, b);
+  return PI_OK;
+}
+
+int pi_element_gradients(pi_kgrid kg, pi_batch b, const void* d_Jw, const double* W, float* d_tri_grad,
+                         float* d_surf_grad, void* d_ws, size_t ws_bytes, pi_stream stream) {
+  if (!kg || !b || !W || (b->n_obj > 0 && !d_Jw)) return fail(PI_ERR_INVALID_ARGUMENT, "pi_element_gradients: bad arguments");
+  if (b->n_obj == 0) return PI_OK;
+  cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  float *tg = nullptr, *sg = nullptr;
+  int rc = launch_adjoint_elements(kg, b, static_cast<const float2*>(d_Jw), W, &tg, &sg, d_ws, ws_bytes, s);
+  if (rc) return rc;
+  if (d_tri_grad && b->n_tri)
+    PI_CUDA(cudaMemcpyAsync(d_tri_grad, tg, b->n_tri * 9 * sizeof(float), cudaMemcpyDeviceToDevice, s));
+  if (d_surf_grad && b->n_surf)
+    PI_CUDA(cudaMemcpyAsync(d_surf_grad, sg, b->n_surf * 12 * sizeof(float), cudaMemcpyDeviceToDevice, s));
+  return PI_OK;
+}
+
+int pi_dof_gradients(pi_kgrid kg, pi_batch b, const void* d_Jw, const double* W, double* d_grad, void* d_ws,
+                     size_t ws_bytes, pi_stream stream) {
+  if (!kg || !b || !W || (b->n_obj > 0 && (!d_Jw || !d_grad)))
+    return fail(PI_ERR_INVALID_ARGUMENT, "pi_dof_gradients: bad arguments");
+  if (b->n_obj == 0) return PI_OK;
+  return launch_dof_gradients(kg, b, static_cast<const float2*>(d_Jw), W, d_grad, d_ws, ws_bytes,
+                              reinterpret_cast<cudaStream_t>(stream));
 }
 
 int pi_volume_matrix_host(const pi_object* objs, int n, const double* dirs, const double* kmag, const double* w,
@@ -327,6 +437,80 @@ int pi_pair_volume_host(const pi_object* o1, const pi_object* o2, const double* 
   int rc = pi_volume_matrix_host(objs, 2, dirs, kmag, w, Q, PI_VOLUME_ONLY, PI_CONTRACT_FP32, V);
   if (rc) return rc;
   *volume = V[1];
+  return PI_OK;
+}
+
+// Shared body of the gradient drop-ins: volumes of all pairs plus, for every
+// j in `cols`, dV_ij/dtheta_i for all i (one adjoint pass with C = ones in
+// column j, i.e. cotangent B_i = A_j for every i).
+static int volume_and_grads_host(const pi_object* objs, int n, const double* dirs, const double* kmag,
+                                 const double* w, int64_t Q, double* V_out, const std::vector<int>& cols,
+                                 std::vector<std::vector<double>>* grads) {
+  cudaStream_t s = cudaStreamPerThread;
+  KGridGuard kg;
+  int rc = pi_kgrid_create(dirs, kmag, w, Q, &kg.k);
+  if (rc) return rc;
+  BatchGuard b;
+  rc = pi_batch_create(objs, n, 0, reinterpret_cast<pi_stream>(s), &b.b);
+  if (rc) return rc;
+  size_t ws_c = 0, ws_a = 0;
+  if ((rc = pi_contract_workspace_size(kg.k, n, PI_CONTRACT_FP32, &ws_c)) || (rc = pi_adjoint_workspace_size(kg.k, b.b, &ws_a)))
+    return rc;
+  const int64_t ng = dof_gradient_size(b.b);
+  DevBuf J, ws, V, G;
+  if ((rc = J.alloc((size_t)n * Q * sizeof(float2), s)) || (rc = ws.alloc(std::max(ws_c, ws_a), s)) ||
+      (rc = V.alloc((size_t)n * n * sizeof(double), s)) || (rc = G.alloc((size_t)std::max<int64_t>(ng, 1) * sizeof(double), s)))
+    return rc;
+  if ((rc = pi_form_factors(kg.k, b.b, 1, J.p, reinterpret_cast<pi_stream>(s)))) return rc;
+  if ((rc = pi_contract(kg.k, J.p, n, PI_CONTRACT_FP32, static_cast<double*>(V.p), ws.p, std::max(ws_c, ws_a),
+                        reinterpret_cast<pi_stream>(s))))
+    return rc;
+  PI_CUDA(cudaMemcpyAsync(V_out, V.p, (size_t)n * n * sizeof(double), cudaMemcpyDeviceToHost, s));
+  grads->assign(cols.size(), std::vector<double>(ng));
+  std::vector<double> C((size_t)n * n);
+  for (size_t c = 0; c < cols.size(); ++c) {
+    std::fill(C.begin(), C.end(), 0.0);
+    for (int i = 0; i < n; ++i) C[(size_t)i * n + cols[c]] = 1.0;  // B_i = A_col for every i
+    if ((rc = pi_dof_gradients(kg.k, b.b, J.p, C.data(), static_cast<double*>(G.p), ws.p, std::max(ws_c, ws_a),
+                               reinterpret_cast<pi_stream>(s))))
+      return rc;
+    PI_CUDA(cudaMemcpyAsync((*grads)[c].data(), G.p, ng * sizeof(double), cudaMemcpyDeviceToHost, s));
+    PI_CUDA(cudaStreamSynchronize(s));
+  }
+  PI_CUDA(cudaStreamSynchronize(s));
+  return PI_OK;
+}
+
+int pi_pair_volume_grad_host(const pi_object* o1, const pi_object* o2, const double* dirs, const double* kmag,
+                             const double* w, int64_t Q, double* volume, double* grad1, double* grad2) {
+  if (!o1 || !o2 || !volume) return fail(PI_ERR_INVALID_ARGUMENT, "pi_pair_volume_grad_host: bad arguments");
+  pi_object objs[2] = {*o1, *o2};
+  double V[4];
+  std::vector<std::vector<double>> g;
+  // column 1: B_0 = A_1 -> dV_01/dtheta_0;  column 0: B_1 = A_0 -> dV_10/dtheta_1
+  int rc = volume_and_grads_host(objs, 2, dirs, kmag, w, Q, V, {1, 0}, &g);
+  if (rc) return rc;
+  *volume = V[1];
+  if (grad1) std::copy(g[0].begin(), g[0].begin() + o1->n_dofs, grad1);
+  if (grad2) std::copy(g[1].begin() + o1->n_dofs, g[1].begin() + o1->n_dofs + o2->n_dofs, grad2);
+  return PI_OK;
+}
+
+int pi_volume_matrix_grad_host(const pi_object* objs, int n, const double* dirs, const double* kmag, const double* w,
+                               int64_t Q, double* V_out, double* grad_out) {
+  if (n <= 0 || !objs || !V_out || !grad_out) return fail(PI_ERR_INVALID_ARGUMENT, "pi_volume_matrix_grad_host: bad arguments");
+  std::vector<int> cols(n);
+  std::iota(cols.begin(), cols.end(), 0);
+  std::vector<std::vector<double>> g;
+  int rc = volume_and_grads_host(objs, n, dirs, kmag, w, Q, V_out, cols, &g);
+  if (rc) return rc;
+  // grad_out block (i, j) = dV_ij/dtheta_i at offset n*goff_i + j*d_i
+  int64_t goff = 0;
+  for (int i = 0; i < n; ++i) {
+    const int64_t d = objs[i].n_dofs;
+    for (int j = 0; j < n; ++j) std::copy(g[j].begin() + goff, g[j].begin() + goff + d, grad_out + n * goff + j * d);
+    goff += d;
+  }
   return PI_OK;
 }
 

@@ -33,6 +33,7 @@ namespace {
 
 constexpr int TC_M = 128;                       // tile edge (objects)
 constexpr int TC_STAGES = 3;
+constexpr int TC_MAX_CHUNKS = 16;                // K stages per CTA (accumulation-error bound)
 constexpr int TC_PWARPS = 8;                    // producer warps
 constexpr int TC_THREADS = (TC_PWARPS + 1) * 32;
 constexpr int BLK_BYTES = TC_M * 128;           // 16 KB: one operand block, 128-byte K rows
@@ -226,38 +227,55 @@ syrk_split3_kernel(const float* __restrict__ X, int n, int64_t K, int nt, int64_
   const uint32_t tmem = tmem_slot;
 
   if (warp < TC_PWARPS) {
-    // ---------------- producers: FP32 -> bf16 hi/lo, swizzled K-major tiles ----------------
+    // ---------------- producers: FP32 -> hi/lo split, swizzled K-major tiles ----------------
+    // Every thread owns UPT 16-byte output chunks per stage; the FP32 inputs of
+    // the next stage are loaded (all of them at once) before the current stage
+    // is converted, so global-load latency overlaps the conversion.
     constexpr int EPC = Kind<KIND>::EPC;
-    constexpr int KC = 8 * EPC;                          // K elements per stage
-    const int units = diag ? TC_M * 8 : 2 * TC_M * 8;  // 16-byte output chunks per stage
+    constexpr int KC = 8 * EPC;                                  // K elements per stage
+    constexpr int UPT = 2 * TC_M * 8 / (TC_PWARPS * 32);         // chunks per thread (off-diagonal pair)
+    const int upt = diag ? UPT / 2 : UPT;
     const bool vec = (K & 3) == 0;
-    for (int64_t c = 0; c < nc; ++c) {
-      const int s = (int)(c % TC_STAGES);
-      const int64_t r = c / TC_STAGES;
-      if (r > 0 && !mbar_wait(smem_u32(&empty_bar[s]), (uint32_t)((r - 1) & 1), err, ERR_PRODUCER_WAIT)) break;
-      uint8_t* st = smem + s * STAGE_BYTES;
+    float xa[UPT][EPC], xb[UPT][EPC];
+    auto load = [&](float (&x)[UPT][EPC], int64_t c) {
       const int64_t kbase = (c0 + c) * KC;
-      for (int u = tid; u < units; u += TC_PWARPS * 32) {
+#pragma unroll
+      for (int i = 0; i < UPT; ++i) {
+        if (i >= upt) break;
+        const int u = tid + i * TC_PWARPS * 32;
         const int blk = u >= TC_M * 8;
         const int uu = u - blk * TC_M * 8;
         const int row = uu >> 3, ch = uu & 7;
         const int grow = (blk ? bj : bi) * TC_M + row;
         const int64_t kk = kbase + ch * EPC;
-        float x[EPC];
         if (vec && grow < n && kk + EPC <= K) {  // 16-byte aligned: K % 4 == 0 and kk % 4 == 0
           const float4* src = reinterpret_cast<const float4*>(X + (int64_t)grow * K + kk);
 #pragma unroll
           for (int v = 0; v < EPC / 4; ++v) {
             const float4 a = __ldg(src + v);
-            x[4 * v] = a.x; x[4 * v + 1] = a.y; x[4 * v + 2] = a.z; x[4 * v + 3] = a.w;
+            x[i][4 * v] = a.x; x[i][4 * v + 1] = a.y; x[i][4 * v + 2] = a.z; x[i][4 * v + 3] = a.w;
           }
         } else {
 #pragma unroll
-          for (int i = 0; i < EPC; ++i) x[i] = (grow < n && kk + i < K) ? X[(int64_t)grow * K + kk + i] : 0.f;
+          for (int e = 0; e < EPC; ++e) x[i][e] = (grow < n && kk + e < K) ? X[(int64_t)grow * K + kk + e] : 0.f;
         }
+      }
+    };
+    auto store = [&](const float (&x)[UPT][EPC], int64_t c) -> bool {
+      const int s = (int)(c % TC_STAGES);
+      const int64_t r = c / TC_STAGES;
+      if (r > 0 && !mbar_wait(smem_u32(&empty_bar[s]), (uint32_t)((r - 1) & 1), err, ERR_PRODUCER_WAIT)) return false;
+      uint8_t* st = smem + s * STAGE_BYTES;
+#pragma unroll
+      for (int i = 0; i < UPT; ++i) {
+        if (i >= upt) break;
+        const int u = tid + i * TC_PWARPS * 32;
+        const int blk = u >= TC_M * 8;
+        const int uu = u - blk * TC_M * 8;
+        const int row = uu >> 3, ch = uu & 7;
         uint4 hi, lo;
-        if (KIND == KIND_BF16) split8(x, &hi, &lo);
-        else split4_tf32(x, &hi, &lo);
+        if (KIND == KIND_BF16) split8(x[i], &hi, &lo);
+        else split4_tf32(x[i], &hi, &lo);
         const uint32_t off = (uint32_t)((row >> 3) * 1024 + (row & 7) * 128 + ((ch ^ (row & 7)) << 4));
         uint8_t* base = st + (blk ? 2 * BLK_BYTES : 0);
         *reinterpret_cast<uint4*>(base + off) = hi;
@@ -266,6 +284,15 @@ syrk_split3_kernel(const float* __restrict__ X, int n, int64_t K, int nt, int64_
       fence_proxy_async();
       __syncwarp();
       if (lane == 0) mbar_arrive(smem_u32(&full_bar[s]));
+      return true;
+    };
+    if (nc > 0) load(xa, 0);
+    for (int64_t c = 0; c < nc; c += 2) {
+      if (c + 1 < nc) load(xb, c + 1);
+      if (!store(xa, c)) break;
+      if (c + 1 >= nc) break;
+      if (c + 2 < nc) load(xa, c + 2);
+      if (!store(xb, c + 1)) break;
     }
   } else if (lane == 0) {
     // ---------------- MMA issuer ----------------
@@ -331,6 +358,7 @@ __global__ void reduce_tc_tiles_kernel(const float* __restrict__ partials, int n
   const int i = bi * TC_M + r, j = bj * TC_M + c;
   if (i >= n || j >= n || (bi == bj && r > c)) return;
   double s = 0.0;
+#pragma unroll 8
   for (int sp = 0; sp < nsplit; ++sp) s += (double)partials[((int64_t)sp * npairs + p) * (TC_M * TC_M) + e];
   s = (*err != 0) ? __longlong_as_double(0x7ff8000000000000LL) : s * INV8PI3;
   V[(int64_t)i * n + j] = s;
@@ -348,7 +376,11 @@ TcPlan plan_tc(int64_t Q, int n, int kind) {
   p.nchunks = (p.K + kc - 1) / kc;
   int dev = 0, sms = 148;
   if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  // At least one CTA per SM, and at most TC_MAX_CHUNKS chunks (48-96 MMAs
+  // each) per accumulator: the tensor cores' FP32 accumulation error grows
+  // with the number of MMAs summed into one accumulator.
   int64_t nsplit = std::max<int64_t>(1, sms / p.npairs);
+  nsplit = std::max<int64_t>(nsplit, (p.nchunks + TC_MAX_CHUNKS - 1) / TC_MAX_CHUNKS);
   nsplit = std::min<int64_t>(nsplit, p.nchunks);
   p.cps = (p.nchunks + nsplit - 1) / nsplit;
   p.nsplit = (int)((p.nchunks + p.cps - 1) / p.cps);

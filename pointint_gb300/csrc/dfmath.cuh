@@ -3,11 +3,11 @@
 // Phases k.x reach 1e4-1e5 rad on the configs' k-grids (k up to ~7e3, centres
 // up to ~14 from the origin).  A plain FP32 phase would carry ~1e-2 rad of
 // error there, so phases are formed as double-float (hi + lo FP32 pair) products
-// and reduced modulo 2 pi by the Cody-Waite method (W. J. Cody and W. Waite,
+// and reduced modulo pi/2 by the Cody-Waite method (W. J. Cody and W. Waite,
 // "Software Manual for the Elementary Functions", 1980) with a two-part split
-// of 2 pi computed from its decimal expansion below, before the hardware
-// sin/cos is applied on [-pi, pi].  Error-free product / sum transformations
-// follow Dekker (1971) and Knuth (TAOCP vol. 2, 4.2.2).
+// of pi/2 computed from its decimal expansion below, then sin and cos come
+// from short polynomials on [-pi/4, pi/4].  Error-free product / sum
+// transformations follow Dekker (1971) and Knuth (TAOCP vol. 2, 4.2.2).
 #pragma once
 #include <cuda_runtime.h>
 #include <cstdint>
@@ -48,8 +48,8 @@ __device__ __forceinline__ df operator*(df a, float s) {  // a * s for s = +-1 o
   return {a.hi * s, a.lo * s};
 }
 
-// a * b as an unnormalised pair (hi, lo) -- enough for reduce_2pi, which
-// treats hi and lo separately.
+// a * b as an unnormalised pair (hi, lo) -- enough for cis, which treats hi
+// and lo separately.
 __device__ __forceinline__ df df_mul_un(df a, df b) {
   const float p = a.hi * b.hi;
   return {p, fmaf(a.hi, b.lo, fmaf(a.lo, b.hi, fmaf(a.hi, b.hi, -p)))};
@@ -69,31 +69,37 @@ __device__ __forceinline__ df cdot(float3 dh, float3 dl, float3 x) {
   return quick_two_sum(t.hi, lo);
 }
 
-// 2 pi = 6.28318530717958647692528676655900576839...
-//   TWO_PI_A = FP32(2 pi)                      = 6.28318548202514648437500
-//   TWO_PI_B = FP32(2 pi - TWO_PI_A)           = -1.7484555314695172e-07
-// |2 pi - A - B| < 1e-14, so n * (2 pi - A - B) < 1e-9 for |n| < 1e5.
-#define PI_TWO_PI_A 6.28318548202514648437500f
-#define PI_TWO_PI_B (-1.7484555314695172e-07f)
-#define PI_INV_TWO_PI 0.15915493667125702f
-
-// Reduces a double-float phase to r in about [-pi, pi] with absolute error
-// ~3e-7 rad for |x| < 2^17; fmaf(-n, A, x) is exact because the result has at
-// most 24 significant bits (n integer, ulp(A) = 2^-21).
-__device__ __forceinline__ float reduce_2pi(df x) {
-  float n = rintf(x.hi * PI_INV_TWO_PI);
-  float r = fmaf(-n, PI_TWO_PI_A, x.hi);
-  r = fmaf(-n, PI_TWO_PI_B, r);
-  return r + x.lo;
-}
+// pi/2 = 1.57079632679489661923132169163975144209858...
+//   PIO2_A = FP32(pi/2)            = 1.5707963705062866
+//   PIO2_B = FP32(pi/2 - PIO2_A)   = -4.371138828673793e-08
+// |pi/2 - A - B| < 2e-15, so n (pi/2 - A - B) < 2e-10 for |n| < 1e5.
+#define PI_PIO2_A 1.5707963705062866f
+#define PI_PIO2_B (-4.371138828673793e-08f)
+#define PI_TWO_OVER_PI 0.6366197466850281f
 
 struct cf { float re, im; };
 
-__device__ __forceinline__ cf cis(df phase) {  // e^{i phase}
-  float r = reduce_2pi(phase);
-  float s, c;
-  __sincosf(r, &s, &c);
-  return {c, s};
+// e^{i x} for a double-float phase x (|x| < ~1e5): Cody-Waite reduction by
+// pi/2 to r in [-pi/4, pi/4] (fmaf(-n, A, x) is exact: the result needs at
+// most 23 significant bits), then this project's own least-squares
+// polynomials for sin(r)/r (degree 4 in r^2) and cos(r) (degree 5 in r^2),
+// fitted on Chebyshev-spaced samples of [-pi/4, pi/4]; FP32 evaluation error
+// <= 7e-8 each, about 5x below the hardware sin/cos approximation.  The
+// quadrant n mod 4 rotates the result.
+__device__ __forceinline__ cf cis(df x) {
+  const float n = rintf(x.hi * PI_TWO_OVER_PI);
+  float r = fmaf(-n, PI_PIO2_A, x.hi);
+  r = fmaf(-n, PI_PIO2_B, r);
+  r += x.lo;
+  const float t = r * r;
+  const float sn = r * fmaf(t, fmaf(t, fmaf(t, fmaf(t, 2.717349162e-06f, -1.983920229e-04f), 8.333329111e-03f),
+                                     -1.666666716e-01f), 1.0f);
+  const float cs = fmaf(t, fmaf(t, fmaf(t, fmaf(t, fmaf(t, -2.717345637e-07f, 2.479892828e-05f), -1.388887991e-03f),
+                                      4.166666791e-02f), -0.5f), 1.0f);
+  const int q = __float2int_rn(n) & 3;
+  const float s1 = (q & 1) ? cs : sn;   // sin(r + q pi/2) up to sign
+  const float c1 = (q & 1) ? sn : cs;   // cos(r + q pi/2) up to sign
+  return {((q + 1) & 2) ? -c1 : c1, (q & 2) ? -s1 : s1};
 }
 
 __device__ __forceinline__ cf cmul(cf a, cf b) { return {a.re * b.re - a.im * b.im, a.re * b.im + a.im * b.re}; }

@@ -92,6 +92,13 @@ struct pi_batch_impl {
   float4* d_surf_pool = nullptr;
   ObjDev* d_objs = nullptr;
   int32_t* d_order = nullptr;
+  // TriangleMeshDoF vertex adjacency (CSR over every mesh object's vertices):
+  // row[v]..row[v+1] index ent[] = pool triangle * 3 + slot; vmap[v] = offset of
+  // the vertex's 3 gradient entries in the concatenated DoF-gradient vector.
+  int64_t n_mesh_verts = 0;
+  int64_t* d_vrow = nullptr;
+  int64_t* d_vent = nullptr;
+  int64_t* d_vmap = nullptr;
   BatchDev dev() const {
     BatchDev b;
     b.n_obj = n_obj; b.objs = d_objs; b.order = d_order; b.tri_pool = d_tri_pool; b.surf_pool = d_surf_pool;
@@ -109,7 +116,12 @@ int launch_contract_fp32(const pi_kgrid_impl* kg, const float2* Jw, int n, doubl
 size_t contract_tc_ws_bytes(int64_t Q, int n, int kind);  // kind 0 = BF16 split, 1 = TF32 split
 int launch_contract_tc(const pi_kgrid_impl* kg, const float2* Jw, int n, int kind, double* V, void* ws,
                        size_t ws_bytes, cudaStream_t s);
-int launch_pair_dot(const pi_kgrid_impl* kg, const float2* Jw, double* d_out, void* ws, cudaStream_t s);
+int64_t dof_gradient_size(const pi_batch_impl* b);
+size_t adjoint_ws_bytes(const pi_kgrid_impl* kg, const pi_batch_impl* b);
+int launch_adjoint_elements(const pi_kgrid_impl* kg, const pi_batch_impl* b, const float2* Jw, const double* W_host,
+                            float** tri_g, float** surf_g, void* ws, size_t ws_bytes, cudaStream_t s);
+int launch_dof_gradients(const pi_kgrid_impl* kg, pi_batch_impl* b, const float2* Jw, const double* W_host,
+                         double* grad, void* ws, size_t ws_bytes, cudaStream_t s);
 int launch_to_double2(const float2* J, int64_t n, double* out, cudaStream_t s);
 
 }  // namespace pi

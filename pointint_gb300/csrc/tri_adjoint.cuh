@@ -1,0 +1,110 @@
+// Vertex-phase derivatives of the triangle form factor (device math of the
+// triangle adjoint, shared with host-side numerical checks).
+#pragma once
+#include "dfmath.cuh"
+
+namespace pi {
+
+// A_tri = -2 gamma F with gamma = khat . S and F = e[pa, pb, pc] (second
+// divided difference of e^{iz} at the vertex phases).  With D_v = dF/dp_v =
+// e[.., p_v, p_v, ..] (one node repeated) and dp_v/dv = k:
+//   dA/dv = -2 ( grad_v(gamma) F + gamma k D_v ),
+// grad_v0 gamma = khat x (e2 - e1)/2, grad_v1 gamma = -khat x e2/2,
+// grad_v2 gamma = khat x e1/2 (reference formula,
+// cpp/src/dof/triangle_mesh_dof.cpp:119-133).  D_a + D_b + D_c = i F.
+//
+// Small spread (D < 2): expansion about the centroid phase pm,
+//   F   = e^{i pm} sum_m i^{m+2} h_m / (m+2)!,
+//   D_v = e^{i pm} sum_m i^{m+3} h_m^(v) / (m+3)!,  h_m^(v) = h_m + d_v h_{m-1}^(v),
+// truncated after m = 12.
+// Large spread: with (P, Q, R) as in tri_generic and G(h) = (e^{ih}-1-ih)/h^2,
+//   f[u,u,v] = e^{iu} G(v-u),
+//   D_R = (f[R,R,Q] - f[P,R,R]) / (Q-P),  D_Q = (f[R,Q,Q] - F) / (Q-P),
+//   D_P = (F - f[P,P,R]) / (Q-P).
+struct TriDer { cf F, Da, Db, Dc; };
+
+__device__ __forceinline__ cf imul(cf a) { return {-a.im, a.re}; }  // i a
+
+__device__ __forceinline__ TriDer tri_series_der(cf P, float al, float be) {
+  const float da = -(al + be) * (1.0f / 3.0f);
+  const float db = al + da, dc = be + da;
+  const float me2 = 0.5f * (da * da + db * db + dc * dc);
+  const float e3 = da * db * dc;
+  float h[13];
+  h[0] = 1.f; h[1] = 0.f; h[2] = me2; h[3] = e3;
+#pragma unroll
+  for (int m = 4; m <= 12; ++m) h[m] = fmaf(me2, h[m - 2], e3 * h[m - 3]);
+  // i^{m+2}/(m+2)!  and  i^{m+3}/(m+3)!  split into real / imaginary parts
+  const float inv_fact[16] = {1.f, 1.f, 0.5f, 1.f / 6, 1.f / 24, 1.f / 120, 1.f / 720, 1.f / 5040, 1.f / 40320,
+                              1.f / 362880, 1.f / 3628800, 1.f / 39916800, 1.f / 479001600, 1.f / 6227020800.f,
+                              1.f / 87178291200.f, 1.f / 1307674368000.f};
+  float Fre = 0.f, Fim = 0.f;
+#pragma unroll
+  for (int m = 0; m <= 12; ++m) {
+    const int p = (m + 2) & 3;  // i^p: 0 -> 1, 1 -> i, 2 -> -1, 3 -> -i
+    const float t = h[m] * inv_fact[m + 2];
+    if (p == 0) Fre += t; else if (p == 1) Fim += t; else if (p == 2) Fre -= t; else Fim -= t;
+  }
+  float hb = 1.f, hc = 1.f;  // h^(v)_0
+  float Bre = 0.f, Bim = 0.f, Cre = 0.f, Cim = 0.f;
+#pragma unroll
+  for (int m = 0; m <= 12; ++m) {
+    if (m > 0) { hb = fmaf(db, hb, h[m]); hc = fmaf(dc, hc, h[m]); }
+    const int p = (m + 3) & 3;
+    const float f = inv_fact[m + 3];
+    const float tb = hb * f, tc = hc * f;
+    if (p == 0) { Bre += tb; Cre += tc; } else if (p == 1) { Bim += tb; Cim += tc; }
+    else if (p == 2) { Bre -= tb; Cre -= tc; } else { Bim -= tb; Cim -= tc; }
+  }
+  TriDer d;
+  d.F = cmul(P, cf{Fre, Fim});
+  d.Db = cmul(P, cf{Bre, Bim});
+  d.Dc = cmul(P, cf{Cre, Cim});
+  const cf iF = imul(d.F);
+  d.Da = {iF.re - d.Db.re - d.Dc.re, iF.im - d.Db.im - d.Dc.im};
+  return d;
+}
+
+// G(h) = (e^{ih} - 1 - ih)/h^2 given E = e^{ih}.
+__device__ __forceinline__ cf Gfun(cf E, float h) {
+  if (fabsf(h) >= 0.5f) {
+    const float ih2 = __frcp_rn(h * h);
+    return {(E.re - 1.0f) * ih2, (E.im - h) * ih2};
+  }
+  // sum_m i^{m+2} h^m/(m+2)!, m = 0..9:
+  //   Re = -1/2 + h^2/24 - h^4/720 + h^6/40320 - h^8/3628800
+  //   Im = h (-1/6 + h^2/120 - h^4/5040 + h^6/362880 - h^8/39916800)
+  const float h2 = h * h;
+  const float re = fmaf(h2, fmaf(h2, fmaf(h2, fmaf(h2, -1.0f / 3628800.0f, 1.0f / 40320.0f), -1.0f / 720.0f),
+                                 1.0f / 24.0f), -0.5f);
+  const float im = h * fmaf(h2, fmaf(h2, fmaf(h2, fmaf(h2, -1.0f / 39916800.0f, 1.0f / 362880.0f), -1.0f / 5040.0f),
+                                     1.0f / 120.0f), -1.0f / 6.0f);
+  return {re, im};
+}
+
+__device__ __forceinline__ cf conjmul(cf a, cf b) { return {a.re * b.re + a.im * b.im, a.im * b.re - a.re * b.im}; }  // a conj(b)
+
+__device__ __forceinline__ TriDer tri_generic_der(cf Pa, cf Pb, cf Pc, float al, float be) {
+  TriDer d;
+  d.F = tri_generic(Pa, Pb, Pc, al, be);
+  const float gab = al, gac = be, gbc = be - al;
+  // vertices as (phasor, relative phase): a = 0, b = al, c = be
+  int P, Q, R;
+  if (fabsf(gab) >= fabsf(gac) && fabsf(gab) >= fabsf(gbc)) { P = 0; Q = 1; R = 2; }
+  else if (fabsf(gac) >= fabsf(gbc)) { P = 0; Q = 2; R = 1; }
+  else { P = 1; Q = 2; R = 0; }
+  const cf ph[3] = {Pa, Pb, Pc};
+  const float z[3] = {0.f, al, be};
+  const float iden = __frcp_rn(z[Q] - z[P]);
+  // f[u,u,v] = e^{iu} G(v - u), e^{i(v-u)} = Pv conj(Pu)
+  auto fuuv = [&](int u, int v) { return cmul(ph[u], Gfun(conjmul(ph[v], ph[u]), z[v] - z[u])); };
+  const cf fRRQ = fuuv(R, Q), fRRP = fuuv(R, P), fQQR = fuuv(Q, R), fPPR = fuuv(P, R);
+  cf D[3];
+  D[R] = cscale(csub(fRRQ, fRRP), iden);
+  D[Q] = cscale(csub(fQQR, d.F), iden);
+  D[P] = cscale(csub(d.F, fPPR), iden);
+  d.Da = D[0]; d.Db = D[1]; d.Dc = D[2];
+  return d;
+}
+
+}  // namespace pi
