@@ -153,12 +153,42 @@ __global__ void prepare_elems_kernel(const PrepObj* objs, const ObjDev* od, floa
   }
 }
 
-constexpr int FF_THREADS = 256;
+constexpr int FF_THREADS = 128;
 constexpr int FF_WARPS = FF_THREADS / 32;
 constexpr int FF_TILE = 256;  // elements staged per shared-memory tile
+constexpr int FF_CHUNK = 16;  // elements summed in FP32 before the compensated outer sum
+
+// Sums over thousands of elements: each thread adds FF_CHUNK element terms into
+// a fresh FP32 partial, then adds the partial to a Kahan-compensated running
+// sum, so rounding does not grow with the element count (a plain FP32 sum over
+// 1,280 triangles measured ~1e-6 of max|A| per node).
+template <int R>
+struct Acc {
+  float re[R], im[R];     // current chunk
+  float sre[R], sim[R];   // running sum
+  float cre[R], cim[R];   // Kahan compensation
+  __device__ __forceinline__ void init() {
+#pragma unroll
+    for (int i = 0; i < R; ++i) { re[i] = im[i] = sre[i] = sim[i] = cre[i] = cim[i] = 0.f; }
+  }
+  __device__ __forceinline__ void flush() {
+#pragma unroll
+    for (int i = 0; i < R; ++i) {
+      float y = re[i] - cre[i], t = sre[i] + y;
+      cre[i] = (t - sre[i]) - y;
+      sre[i] = t;
+      y = im[i] - cim[i];
+      t = sim[i] + y;
+      cim[i] = (t - sim[i]) - y;
+      sim[i] = t;
+      re[i] = 0.f;
+      im[i] = 0.f;
+    }
+  }
+};
 
 template <int R>
-__global__ void __launch_bounds__(FF_THREADS, 2)
+__global__ void __launch_bounds__(FF_THREADS, 3)
 ff_kernel(KGridDev kg, BatchDev b, float2* __restrict__ J, int scale_sqrt_w) {
   const int oi = b.order[blockIdx.y];
   const ObjDev od = b.objs[oi];
@@ -186,9 +216,8 @@ ff_kernel(KGridDev kg, BatchDev b, float2* __restrict__ J, int scale_sqrt_w) {
     float2 k = (active && r < kg.L) ? kg.kmag[r] : make_float2(0.f, 0.f);
     km[i] = df{k.x, k.y};
   }
-  float acc_re[R], acc_im[R];
-#pragma unroll
-  for (int i = 0; i < R; ++i) { acc_re[i] = 0.f; acc_im[i] = 0.f; }
+  Acc<R> acc;
+  acc.init();
 
   __shared__ float4 tile[3 * FF_TILE];
   const int n = od.n_elems;
@@ -222,10 +251,10 @@ ff_kernel(KGridDev kg, BatchDev b, float2* __restrict__ J, int scale_sqrt_w) {
             gmask |= (tay ? 0u : 1u) << i;
             const cf S = tri_series_eval(tp, km[i].hi);
             const cf P = cis(df_mul_un(km[i], sm));
-            const float re = fmaf(P.re, S.re, fmaf(-P.im, S.im, acc_re[i]));
-            const float im = fmaf(P.re, S.im, fmaf(P.im, S.re, acc_im[i]));
-            acc_re[i] = tay ? re : acc_re[i];
-            acc_im[i] = tay ? im : acc_im[i];
+            const float re = fmaf(P.re, S.re, fmaf(-P.im, S.im, acc.re[i]));
+            const float im = fmaf(P.re, S.im, fmaf(P.im, S.re, acc.im[i]));
+            acc.re[i] = tay ? re : acc.re[i];
+            acc.im[i] = tay ? im : acc.im[i];
           }
           if (gmask) {
             // Large-spread radii: vertex phases in double-float
@@ -238,11 +267,12 @@ ff_kernel(KGridDev kg, BatchDev b, float2* __restrict__ J, int scale_sqrt_w) {
               if (gmask & (1u << i)) {
                 const cf v = tri_generic(cis(df_mul(km[i], sa)), cis(df_mul(km[i], sb)), cis(df_mul(km[i], sc)),
                                          km[i].hi * d1.hi, km[i].hi * d2.hi);
-                acc_re[i] = fmaf(g, v.re, acc_re[i]);
-                acc_im[i] = fmaf(g, v.im, acc_im[i]);
+                acc.re[i] = fmaf(g, v.re, acc.re[i]);
+                acc.im[i] = fmaf(g, v.im, acc.im[i]);
               }
             }
           }
+          if (((base + e) & (FF_CHUNK - 1)) == FF_CHUNK - 1) acc.flush();
         }
       }
     }
@@ -274,8 +304,8 @@ ff_kernel(KGridDev kg, BatchDev b, float2* __restrict__ J, int scale_sqrt_w) {
               const float S = (x < 1e-10f) ? 1.0f : 2.0f * j1x(x);
               const cf P = cis(df_mul(km[i], sc));
               const float m = S * amp;
-              acc_re[i] = fmaf(m, P.re, acc_re[i]);
-              acc_im[i] = fmaf(m, P.im, acc_im[i]);
+              acc.re[i] = fmaf(m, P.re, acc.re[i]);
+              acc.im[i] = fmaf(m, P.im, acc.im[i]);
             }
           } else {
             const float hs = -0.5f * q0.w * q0.w * perp;
@@ -284,16 +314,18 @@ ff_kernel(KGridDev kg, BatchDev b, float2* __restrict__ J, int scale_sqrt_w) {
               const float k2 = km[i].hi * km[i].hi;
               const float m = __expf(hs * k2) * amp;
               const cf P = cis(df_mul(km[i], sc));
-              acc_re[i] = fmaf(m, P.re, acc_re[i]);
-              acc_im[i] = fmaf(m, P.im, acc_im[i]);
+              acc.re[i] = fmaf(m, P.re, acc.re[i]);
+              acc.im[i] = fmaf(m, P.im, acc.im[i]);
             }
           }
+          if (((base + e) & (FF_CHUNK - 1)) == FF_CHUNK - 1) acc.flush();
         }
       }
     }
   }
 
   if (!active) return;
+  acc.flush();
   // origin phase e^{i k.o}: dir . o formed in FP64 once per thread, then double-float.
   const double dox = (double)dh.x + (double)dl.x, doy = (double)dh.y + (double)dl.y,
                doz = (double)dh.z + (double)dl.z;
@@ -306,7 +338,7 @@ ff_kernel(KGridDev kg, BatchDev b, float2* __restrict__ J, int scale_sqrt_w) {
     const int r = rb + nrb * i;
     if (r < kg.L) {
       const int64_t q = (int64_t)r * kg.M + j;
-      cf v = cmul(cis(df_mul(km[i], so)), cf{acc_re[i], acc_im[i]});
+      cf v = cmul(cis(df_mul(km[i], so)), cf{acc.sre[i], acc.sim[i]});
       if (km[i].hi * dnorm < 1e-10f) v = cf{0.f, 0.f};  // A(0) = 0 (affine_dof.cpp:64-65)
       if (scale_sqrt_w) { const float s = kg.sqrtw[q]; v.re *= s; v.im *= s; }
       J[Jrow + q] = make_float2(v.re, v.im);
@@ -357,14 +389,13 @@ int launch_form_factors(const pi_kgrid_impl* kg, const pi_batch_impl* b, int sca
   if (b->n_obj == 0) return PI_OK;
   const KGridDev K = kg->dev;
   const BatchDev B = b->dev();
-  int R = K.L >= 128 ? 16 : K.L >= 32 ? 8 : K.L >= 4 ? 4 : 1;
+  int R = K.L >= 32 ? 8 : K.L >= 4 ? 4 : 1;
   const int nrb = (K.L + R - 1) / R;
   const int ndt = (K.M + 31) / 32;
   const int64_t items = (int64_t)nrb * ndt;
   dim3 grid((unsigned)((items + FF_WARPS - 1) / FF_WARPS), (unsigned)b->n_obj);
   if (grid.y > 65535) return fail(PI_ERR_UNSUPPORTED, "more than 65535 objects in one batch");
   switch (R) {
-    case 16: ff_kernel<16><<<grid, FF_THREADS, 0, s>>>(K, B, J, scale_sqrt_w); break;
     case 8: ff_kernel<8><<<grid, FF_THREADS, 0, s>>>(K, B, J, scale_sqrt_w); break;
     case 4: ff_kernel<4><<<grid, FF_THREADS, 0, s>>>(K, B, J, scale_sqrt_w); break;
     default: ff_kernel<1><<<grid, FF_THREADS, 0, s>>>(K, B, J, scale_sqrt_w); break;
