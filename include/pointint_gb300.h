@@ -190,6 +190,23 @@ int pi_element_gradients(pi_kgrid kg, pi_batch b, const void* d_Jw, const double
 int pi_dof_gradients(pi_kgrid kg, pi_batch b, const void* d_Jw, const double* W, double* d_grad, void* d_ws,
                      size_t ws_bytes, pi_stream stream);
 
+/* Allocation-free FP32 contraction.  No counterpart in the reference.
+ * For callers that cannot call cudaMalloc -- an application whose device
+ * memory belongs to a host framework's pre-reserved pool, or a latency-
+ * critical loop where an allocation would synchronise the device -- this entry
+ * point allocates nothing: its split-K scratch is a fixed 8 MiB device array
+ * inside the library, held on every GPU that loads the library until the
+ * process exits.  The first call on a device looks up that array's address
+ * with the device current; make that first call before any stream capture.
+ * Inputs and output are caller-owned device buffers: d_Jw is the
+ * sqrt(|w|)-scaled J (complex64, n x Q), d_sign the Q signs of the quadrature
+ * weights or NULL when all are >= 0, d_V the n x n double output (1/(8 pi^3)
+ * applied).  Object counts whose partial tiles exceed 8 MiB (about 1,900
+ * objects on a 152-SM GB300) return PI_ERR_WORKSPACE_TOO_SMALL.  All calls
+ * share the array, so calls whose kernels overlap on the GPU race. */
+int pi_contract_fp32_static(const void* d_Jw, int64_t Q, int n_objects, const float* d_sign, double* d_V,
+                            pi_stream stream);
+
 /* ---- one-shot host-buffer drop-ins ------------------------------------------ */
 /* compute_intersection_volume_matrix_cuda (cpp/include/compute_intersection_volume_multi_object.hpp:51-59).
  * Host objects and k-grid; V_out: host n x n.  flags: PI_VOLUME_ONLY only in

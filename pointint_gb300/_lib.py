@@ -75,6 +75,7 @@ SIGNATURES = {
     "pi_form_factors": (I32, [P, P, I32, P, P]),
     "pi_contract_workspace_size": (I32, [P, I32, I32, ctypes.POINTER(SZ)]),
     "pi_contract": (I32, [P, P, I32, I32, P, P, SZ, P]),
+    "pi_contract_fp32_static": (I32, [P, I64, I32, P, P, P]),
     "pi_batch_set_elements": (I32, [P, I32, P, P]),
     "pi_batch_layout": (I32, [P, I32, ctypes.POINTER(I64), ctypes.POINTER(I64), ctypes.POINTER(I64)]),
     "pi_adjoint_workspace_size": (I32, [P, P, ctypes.POINTER(SZ)]),

@@ -14,6 +14,7 @@
 #include <cuda_runtime.h>
 #include <cstdint>
 #include <algorithm>
+#include <mutex>
 #include "pi_internal.h"
 
 namespace pi {
@@ -173,4 +174,69 @@ int launch_contract_fp32(const pi_kgrid_impl* kg, const float2* Jw, int n, doubl
   return PI_OK;
 }
 
+// ---------------------------------------------------------------------------
+// Allocation-free variant of the FP32 contraction (pi_contract_fp32_static).
+//
+// Some callers cannot call cudaMalloc: applications whose device memory is
+// owned by a host framework (a pool or arena reserved up front, from which a
+// library may not allocate), and latency-critical loops in which a
+// cudaMalloc / cudaFree would synchronise the device.  For them the split-K
+// partial tiles live in this file-scope device array instead of a caller
+// workspace.  Every GPU that loads the library holds these 8 MiB until the
+// process exits.  All calls share the array: two calls whose kernels overlap
+// on the GPU (different streams, or different host threads) race on it and
+// must be ordered by the caller.  The partial tiles are fully written by the
+// first kernel before the second kernel reads them, so nothing in the array
+// needs to start at zero and what the previous call left there is never read.
+// ---------------------------------------------------------------------------
+constexpr size_t PI_STATIC_SCRATCH_BYTES = size_t(8) << 20;  // 8 MiB of partial tiles
+static __device__ __align__(256) float g_static_partials[PI_STATIC_SCRATCH_BYTES / sizeof(float)];
+
+namespace {
+std::mutex g_static_mu;
+float* g_static_ptr[256] = {};  // per device: device address of g_static_partials
+}  // namespace
+
 }  // namespace pi
+
+extern "C" int pi_contract_fp32_static(const void* d_Jw, int64_t Q, int n, const float* d_sign, double* d_V,
+                                       pi_stream stream) {
+  using namespace pi;
+  if (n < 0 || Q <= 0 || (n > 0 && (!d_Jw || !d_V)))
+    return fail(PI_ERR_INVALID_ARGUMENT, "pi_contract_fp32_static: bad arguments");
+  if (n == 0) return PI_OK;
+  int dev = 0;
+  PI_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 256) return fail(PI_ERR_UNSUPPORTED, "pi_contract_fp32_static: device index beyond 255");
+  SyrkPlan p = plan_syrk(Q, n);
+  const size_t need = (size_t)p.nsplit * p.npairs * TB * TB * sizeof(float);
+  if (need > PI_STATIC_SCRATCH_BYTES) {
+    char buf[200];
+    snprintf(buf, sizeof buf,
+             "pi_contract_fp32_static: %d objects need %zu bytes of partial tiles, above the fixed %zu-byte "
+             "device array; use pi_contract with a caller workspace",
+             n, need, PI_STATIC_SCRATCH_BYTES);
+    return fail(PI_ERR_WORKSPACE_TOO_SMALL, buf);
+  }
+  float* scratch = nullptr;
+  {
+    // First call on a device: look up the array's device address with that
+    // device current (host code cannot use the symbol itself as a pointer).
+    std::lock_guard<std::mutex> lock(g_static_mu);
+    if (!g_static_ptr[dev]) {
+      void* ptr = nullptr;
+      cudaError_t e = cudaGetSymbolAddress(&ptr, g_static_partials);
+      if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(g_static_partials)");
+      g_static_ptr[dev] = static_cast<float*>(ptr);
+    }
+    scratch = g_static_ptr[dev];
+  }
+  cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  dim3 grid((unsigned)p.npairs, (unsigned)p.nsplit);
+  syrk_fp32_kernel<<<grid, 256, 0, s>>>(static_cast<const float*>(d_Jw), n, p.K, d_sign, p.nt, p.kchunk, scratch);
+  PI_LAUNCHED("syrk_fp32_kernel");
+  const int64_t total = (int64_t)p.npairs * TB * TB;
+  reduce_tiles_kernel<<<(unsigned)((total + 255) / 256), 256, 0, s>>>(scratch, p.nsplit, p.npairs, p.nt, n, d_V);
+  PI_LAUNCHED("reduce_tiles_kernel");
+  return PI_OK;
+}
