@@ -21,10 +21,12 @@
 // error code in the workspace, stops issuing work, drains its outstanding
 // MMAs, frees its tensor memory and returns; the reduction then writes NaN to
 // V so a failure can never read as a volume.
+#include <cuda.h>
 #include <cuda_runtime.h>
 #include <cuda_bf16.h>
 #include <cstdint>
 #include <algorithm>
+#include <mutex>
 #include "pi_internal.h"
 
 namespace pi {
@@ -34,8 +36,10 @@ namespace {
 constexpr int TC_M = 128;                       // tile edge (objects)
 constexpr int TC_STAGES = 3;
 constexpr int TC_MAX_CHUNKS = 16;                // K stages per CTA (accumulation-error bound)
-constexpr int TC_PWARPS = 8;                    // producer warps
-constexpr int TC_THREADS = (TC_PWARPS + 1) * 32;
+constexpr int TC_PWARPS = 8;                    // converter warps
+constexpr int TC_TMA_WARP = TC_PWARPS;          // lane 0 issues the TMA loads
+constexpr int TC_MMA_WARP = TC_PWARPS + 1;      // lane 0 issues the MMAs; the warp owns TMEM
+constexpr int TC_THREADS = (TC_PWARPS + 2) * 32;
 constexpr int BLK_BYTES = TC_M * 128;           // 16 KB: one operand block, 128-byte K rows
 constexpr int STAGE_BYTES = 4 * BLK_BYTES;      // A hi, A lo, B hi, B lo
 constexpr int SMEM_BYTES = TC_STAGES * STAGE_BYTES + 1024;  // + alignment slack
@@ -58,7 +62,7 @@ constexpr uint32_t idesc() {
          ((uint32_t)(TC_M >> 4) << 24);
 }
 
-enum { ERR_PRODUCER_WAIT = 1, ERR_MMA_WAIT = 2, ERR_EPILOGUE_WAIT = 3 };
+enum { ERR_PRODUCER_WAIT = 1, ERR_MMA_WAIT = 2, ERR_EPILOGUE_WAIT = 3, ERR_TMA_WAIT = 4 };
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
@@ -93,6 +97,41 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, int* er
     }
   }
   return true;
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
+  asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.expect_tx.shared::cta.b64 st, [%0], %1;\n\t}" ::"r"(bar),
+               "r"(bytes)
+               : "memory");
+}
+
+// 2D tiled TMA load of a box of FP32 J (x = K coordinate, a multiple of 4
+// elements = 16 bytes; y = row) into shared memory, completing on `bar`.
+__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map, int x, int y, uint32_t bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::
+          "r"(dst),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(bar)
+      : "memory");
+}
+
+// Bounded wait used only to drain copies already in flight; ignores the flag.
+__device__ __forceinline__ void mbar_drain(uint32_t bar, uint32_t parity) {
+  const long long t0 = clock64();
+  while (!mbar_try_wait(bar, parity) && clock64() - t0 <= WAIT_CYCLES) {
+  }
+}
+
+// Named barrier 1 over the converter warps with an OR-reduction, so every
+// converter takes the same exit decision.
+__device__ __forceinline__ bool converters_any(bool pred) {
+  uint32_t r;
+  asm volatile(
+      "{\n\t.reg .pred p, q;\n\tsetp.ne.b32 q, %1, 0;\n\tbar.red.or.pred p, 1, %2, q;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(r)
+      : "r"((uint32_t)pred), "r"(TC_PWARPS * 32)
+      : "memory");
+  return r != 0;
 }
 
 __device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
@@ -192,9 +231,10 @@ __device__ __forceinline__ void split8(const float* x, uint4* hi, uint4* lo) {
 
 template <int KIND>
 __global__ void __launch_bounds__(TC_THREADS, 1)
-syrk_split3_kernel(const float* __restrict__ X, int n, int64_t K, int nt, int64_t nchunks, int64_t cps,
+syrk_split3_kernel(const __grid_constant__ CUtensorMap xmap, int n, int64_t K, int nt, int64_t nchunks, int64_t cps,
                    float* __restrict__ partials, int* __restrict__ err) {
   extern __shared__ uint8_t smem_raw[];
+  __shared__ __align__(8) uint64_t tma_bar[TC_STAGES];
   __shared__ __align__(8) uint64_t full_bar[TC_STAGES];
   __shared__ __align__(8) uint64_t empty_bar[TC_STAGES];
   __shared__ __align__(8) uint64_t done_bar;
@@ -210,13 +250,14 @@ syrk_split3_kernel(const float* __restrict__ X, int n, int64_t K, int nt, int64_
 
   if (tid == 0) {
     for (int s = 0; s < TC_STAGES; ++s) {
+      mbar_init(smem_u32(&tma_bar[s]), 1);
       mbar_init(smem_u32(&full_bar[s]), TC_PWARPS);
       mbar_init(smem_u32(&empty_bar[s]), 1);
     }
     mbar_init(smem_u32(&done_bar), 1);
     fence_mbar_init();
   }
-  if (warp == TC_PWARPS) {
+  if (warp == TC_MMA_WARP) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_slot)),
                  "r"(TC_M));
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
@@ -226,46 +267,62 @@ syrk_split3_kernel(const float* __restrict__ X, int n, int64_t K, int nt, int64_
   tc_fence_after();
   const uint32_t tmem = tmem_slot;
 
-  if (warp < TC_PWARPS) {
-    // ---------------- producers: FP32 -> hi/lo split, swizzled K-major tiles ----------------
-    // Every thread owns UPT 16-byte output chunks per stage; the FP32 inputs of
-    // the next stage are loaded (all of them at once) before the current stage
-    // is converted, so global-load latency overlaps the conversion.
-    constexpr int EPC = Kind<KIND>::EPC;
-    constexpr int KC = 8 * EPC;                                  // K elements per stage
-    constexpr int UPT = 2 * TC_M * 8 / (TC_PWARPS * 32);         // chunks per thread (off-diagonal pair)
-    const int upt = diag ? UPT / 2 : UPT;
-    const bool vec = (K & 3) == 0;
-    float xa[UPT][EPC], xb[UPT][EPC];
-    auto load = [&](float (&x)[UPT][EPC], int64_t c) {
-      const int64_t kbase = (c0 + c) * KC;
-#pragma unroll
-      for (int i = 0; i < UPT; ++i) {
-        if (i >= upt) break;
-        const int u = tid + i * TC_PWARPS * 32;
-        const int blk = u >= TC_M * 8;
-        const int uu = u - blk * TC_M * 8;
-        const int row = uu >> 3, ch = uu & 7;
-        const int grow = (blk ? bj : bi) * TC_M + row;
-        const int64_t kk = kbase + ch * EPC;
-        if (vec && grow < n && kk + EPC <= K) {  // 16-byte aligned: K % 4 == 0 and kk % 4 == 0
-          const float4* src = reinterpret_cast<const float4*>(X + (int64_t)grow * K + kk);
-#pragma unroll
-          for (int v = 0; v < EPC / 4; ++v) {
-            const float4 a = __ldg(src + v);
-            x[i][4 * v] = a.x; x[i][4 * v + 1] = a.y; x[i][4 * v + 2] = a.z; x[i][4 * v + 3] = a.w;
-          }
-        } else {
-#pragma unroll
-          for (int e = 0; e < EPC; ++e) x[i][e] = (grow < n && kk + e < K) ? X[(int64_t)grow * K + kk + e] : 0.f;
-        }
+  constexpr int EPC = Kind<KIND>::EPC;
+  constexpr int KC = 8 * EPC;                              // K elements per stage
+  constexpr uint32_t BOX_BYTES = TC_M * KC * 4;            // FP32 box of one 128-row block
+  // BF16: the 32 KB FP32 box fills the block's 32 KB hi+lo region; TF32: the
+  // 16 KB box lands in the upper half.  Either way the split is done in place.
+  constexpr uint32_t BOX_OFF = 2 * BLK_BYTES - BOX_BYTES;
+  if (warp == TC_TMA_WARP) {
+    // ---------------- TMA: FP32 J tiles into the stage ring ----------------
+    if (lane == 0) {
+      int64_t issued = 0;
+      for (int64_t c = 0; c < nc; ++c) {
+        const int s = (int)(c % TC_STAGES);
+        const int64_t r = c / TC_STAGES;
+        if (r > 0 && !mbar_wait(smem_u32(&empty_bar[s]), (uint32_t)((r - 1) & 1), err, ERR_TMA_WAIT)) break;
+        const uint32_t st = smem_u32(smem + s * STAGE_BYTES);
+        const int x = (int)((c0 + c) * KC);
+        mbar_expect_tx(smem_u32(&tma_bar[s]), diag ? BOX_BYTES : 2 * BOX_BYTES);
+        tma_load_2d(st + BOX_OFF, &xmap, x, bi * TC_M, smem_u32(&tma_bar[s]));
+        if (!diag) tma_load_2d(st + 2 * BLK_BYTES + BOX_OFF, &xmap, x, bj * TC_M, smem_u32(&tma_bar[s]));
+        issued = c + 1;
       }
-    };
-    auto store = [&](const float (&x)[UPT][EPC], int64_t c) -> bool {
+      // Never leave this CTA with a copy still landing in its shared memory:
+      // wait (bounded) for the last load issued into every stage.
+      for (int64_t c = max((int64_t)0, issued - TC_STAGES); c < issued; ++c)
+        mbar_drain(smem_u32(&tma_bar[c % TC_STAGES]), (uint32_t)((c / TC_STAGES) & 1));
+    }
+  } else if (warp < TC_PWARPS) {
+    // ---------------- converters: FP32 box -> hi/lo split, 128-byte swizzled K-major ----------------
+    constexpr int UPT = 2 * TC_M * 8 / (TC_PWARPS * 32);  // 16-byte output chunks per thread (off-diagonal pair)
+    const int upt = diag ? UPT / 2 : UPT;
+    for (int64_t c = 0; c < nc; ++c) {
       const int s = (int)(c % TC_STAGES);
       const int64_t r = c / TC_STAGES;
-      if (r > 0 && !mbar_wait(smem_u32(&empty_bar[s]), (uint32_t)((r - 1) & 1), err, ERR_PRODUCER_WAIT)) return false;
+      bool ok = mbar_wait(smem_u32(&tma_bar[s]), (uint32_t)(r & 1), err, ERR_PRODUCER_WAIT);
       uint8_t* st = smem + s * STAGE_BYTES;
+      float x[UPT][EPC];
+      if (ok) {
+#pragma unroll
+        for (int i = 0; i < UPT; ++i) {
+          if (i >= upt) break;
+          const int u = tid + i * TC_PWARPS * 32;
+          const int blk = u >= TC_M * 8;
+          const int uu = u - blk * TC_M * 8;
+          const int row = uu >> 3, ch = uu & 7;
+          const float4* src = reinterpret_cast<const float4*>(st + blk * 2 * BLK_BYTES + BOX_OFF + row * (KC * 4) +
+                                                             ch * (EPC * 4));
+#pragma unroll
+          for (int v = 0; v < EPC / 4; ++v) {
+            const float4 a = src[v];
+            x[i][4 * v] = a.x; x[i][4 * v + 1] = a.y; x[i][4 * v + 2] = a.z; x[i][4 * v + 3] = a.w;
+          }
+        }
+      }
+      // every converter has read its inputs before any output overwrites the
+      // box; all converters leave together if any of them saw an error
+      if (converters_any(!ok)) break;
 #pragma unroll
       for (int i = 0; i < UPT; ++i) {
         if (i >= upt) break;
@@ -284,17 +341,8 @@ syrk_split3_kernel(const float* __restrict__ X, int n, int64_t K, int nt, int64_
       fence_proxy_async();
       __syncwarp();
       if (lane == 0) mbar_arrive(smem_u32(&full_bar[s]));
-      return true;
-    };
-    if (nc > 0) load(xa, 0);
-    for (int64_t c = 0; c < nc; c += 2) {
-      if (c + 1 < nc) load(xb, c + 1);
-      if (!store(xa, c)) break;
-      if (c + 1 >= nc) break;
-      if (c + 2 < nc) load(xa, c + 2);
-      if (!store(xb, c + 1)) break;
     }
-  } else if (lane == 0) {
+  } else if (warp == TC_MMA_WARP && lane == 0) {
     // ---------------- MMA issuer ----------------
     for (int64_t c = 0; c < nc; ++c) {
       const int s = (int)(c % TC_STAGES);
@@ -339,7 +387,7 @@ syrk_split3_kernel(const float* __restrict__ X, int n, int64_t K, int nt, int64_
   }
   tc_fence_before();
   __syncthreads();
-  if (warp == TC_PWARPS) {
+  if (warp == TC_MMA_WARP) {
     __syncwarp();
     tc_fence_after();
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TC_M));
@@ -395,10 +443,40 @@ size_t contract_tc_ws_bytes(int64_t Q, int n, int kind) {
   return 256 + (size_t)p.nsplit * p.npairs * TC_M * TC_M * sizeof(float);
 }
 
+namespace {
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+EncodeTiledFn encode_tiled() {
+  static std::once_flag once;
+  static EncodeTiledFn fn = nullptr;
+  std::call_once(once, [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<EncodeTiledFn>(p);
+  });
+  return fn;
+}
+}  // namespace
+
 int launch_contract_tc(const pi_kgrid_impl* kg, const float2* Jw, int n, int kind, double* V, void* ws,
                        size_t ws_bytes, cudaStream_t s) {
   if (n <= 0) return PI_OK;
   TcPlan p = plan_tc(kg->Q, n, kind);
+  if (p.K % 4 != 0) return fail(PI_ERR_UNSUPPORTED, "tensor-core contraction needs an even node count");
+  EncodeTiledFn enc = encode_tiled();
+  if (!enc) return fail(PI_ERR_CUDA, "cuTensorMapEncodeTiled is not available from the driver");
+  CUtensorMap xmap;
+  const cuuint64_t gdim[2] = {(cuuint64_t)p.K, (cuuint64_t)n};
+  const cuuint64_t gstride[1] = {(cuuint64_t)p.K * sizeof(float)};
+  const cuuint32_t box[2] = {(cuuint32_t)(kind == KIND_BF16 ? 64 : 32), (cuuint32_t)TC_M};
+  const cuuint32_t estride[2] = {1, 1};
+  CUresult cr = enc(&xmap, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float2*>(Jw), gdim, gstride, box, estride,
+                    CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                    CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (cr != CUDA_SUCCESS) return fail(PI_ERR_CUDA, "cuTensorMapEncodeTiled failed for J");
   const size_t need = 256 + (size_t)p.nsplit * p.npairs * TC_M * TC_M * sizeof(float);
   if (ws_bytes < need || !ws) return fail(PI_ERR_WORKSPACE_TOO_SMALL, "tensor-core contraction workspace too small");
   if ((reinterpret_cast<uintptr_t>(Jw) & 15) != 0) return fail(PI_ERR_INVALID_ARGUMENT, "J must be 16-byte aligned");
@@ -415,11 +493,11 @@ int launch_contract_tc(const pi_kgrid_impl* kg, const float2* Jw, int n, int kin
   PI_CUDA(cudaMemsetAsync(err, 0, sizeof(int), s));
   dim3 grid((unsigned)p.npairs, (unsigned)p.nsplit);
   if (kind == KIND_BF16)
-    syrk_split3_kernel<KIND_BF16><<<grid, TC_THREADS, SMEM_BYTES, s>>>(reinterpret_cast<const float*>(Jw), n, p.K,
-                                                                      p.nt, p.nchunks, p.cps, partials, err);
+    syrk_split3_kernel<KIND_BF16><<<grid, TC_THREADS, SMEM_BYTES, s>>>(xmap, n, p.K, p.nt, p.nchunks, p.cps,
+                                                                      partials, err);
   else
-    syrk_split3_kernel<KIND_TF32><<<grid, TC_THREADS, SMEM_BYTES, s>>>(reinterpret_cast<const float*>(Jw), n, p.K,
-                                                                      p.nt, p.nchunks, p.cps, partials, err);
+    syrk_split3_kernel<KIND_TF32><<<grid, TC_THREADS, SMEM_BYTES, s>>>(xmap, n, p.K, p.nt, p.nchunks, p.cps,
+                                                                      partials, err);
   PI_LAUNCHED("syrk_split3_kernel");
   const int64_t total = (int64_t)p.npairs * TC_M * TC_M;
   reduce_tc_tiles_kernel<<<(unsigned)((total + 255) / 256), 256, 0, s>>>(partials, p.nsplit, p.npairs, p.nt, n, err, V);
