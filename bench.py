@@ -6,7 +6,7 @@ k-grid L=64 x Lebedev-1202 (N_k = 76,928).  One step = one cold volume matrix
 from device-resident geometry: DoF transform + form factors (5.05e10
 triangle x k evaluations) + contraction V = Re(J^H D J).
 
-    python bench.py [--gpus N --steps K --warmup W] [--impl reference] [--precision fp32|bf16x3]
+    python bench.py [--gpus N --steps K --warmup W] [--impl reference] [--precision fp32|bf16x3|tf32x3|fp16x3]
 
 `value`  : triangle x k evaluations per second over the whole job (inputs
            resident in HBM; L2 flushed before every timed step).
@@ -45,7 +45,7 @@ def parse():
     p.add_argument("--steps", type=int, default=10)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    p.add_argument("--precision", default="auto", choices=["auto", "fp32", "bf16x3", "tf32x3"])
+    p.add_argument("--precision", default="auto", choices=["auto", "fp32", "bf16x3", "tf32x3", "fp16x3"])
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--cpu-seconds", type=float, default=12.0)
@@ -193,7 +193,7 @@ def run_gb300(args):
     n_tri = meta["n_triangles"]
     Q = kg.num_nodes
     evals_step = n_tri * Q
-    precision = "tf32x3" if args.precision == "auto" else args.precision
+    precision = "fp16x3" if args.precision == "auto" else args.precision
     stream = torch.cuda.current_stream()
     batch = core.ObjectBatch(objs)
     Jw = torch.empty((n_obj, Q), dtype=torch.complex64, device="cuda")
@@ -266,16 +266,15 @@ def run_gb300(args):
         return ((Vx - V64).abs() / torch.maximum(V64.abs(), eps * d64)).max().item()
 
     contraction = {"reference": "FP64 contraction of the same J"}
-    for p in ("fp32", "tf32x3", "bf16x3"):
+    for p in ("fp32", "tf32x3", "bf16x3", "fp16x3"):
         try:
             contraction[p] = {"ms": time_contract(p), "max_rel_err": cond_err(V, 1e-3),
                               "max_rel_err_floor_1e-2": cond_err(V, 1e-2)}
         except _lib.PointIntError as exc:
             contraction[p] = {"error": str(exc)}
-    if "ms" in contraction.get("bf16x3", {}) and "ms" in contraction["fp32"]:
-        contraction["speedup_bf16x3_vs_fp32"] = contraction["fp32"]["ms"] / contraction["bf16x3"]["ms"]
-    if "ms" in contraction.get("tf32x3", {}) and "ms" in contraction["fp32"]:
-        contraction["speedup_tf32x3_vs_fp32"] = contraction["fp32"]["ms"] / contraction["tf32x3"]["ms"]
+    for p in ("tf32x3", "bf16x3", "fp16x3"):
+        if "ms" in contraction.get(p, {}) and "ms" in contraction["fp32"]:
+            contraction[f"speedup_{p}_vs_fp32"] = contraction["fp32"]["ms"] / contraction[p]["ms"]
     contraction["error_definition"] = "max_ij |dV_ij| / max(|V_ij|, eps sqrt(V_ii V_jj)), eps = 1e-3 (or 1e-2)"
     del X, V64
 

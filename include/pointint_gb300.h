@@ -57,7 +57,9 @@ enum { PI_VOLUME_ONLY = 1, PI_GRADIENT = 2, PI_HESSIAN = 4, PI_ALL = 7 };
 enum {
   PI_CONTRACT_FP32 = 0,      /* FP32 SIMT (the plain drop-in)                                    */
   PI_CONTRACT_BF16X3 = 1,    /* BF16 hi+lo split on tcgen05 tensor cores, FP32 accumulation      */
-  PI_CONTRACT_TF32X3 = 2     /* TF32 hi+lo split on tcgen05 tensor cores (~21 bits), FP32 accum. */
+  PI_CONTRACT_TF32X3 = 2,    /* TF32 hi+lo split on tcgen05 tensor cores (~21 bits), FP32 accum. */
+  PI_CONTRACT_FP16X3 = 3     /* FP16 hi+lo split of each row scaled by a power of two (~22 bits),
+                                tcgen05 tensor cores, FP32 accumulation                           */
 };
 
 /* ---- packed element layouts (reference cpp/include/geometry/types.hpp:9-37) */

@@ -20,7 +20,7 @@ STATUS_NAMES = {0: "ok", 1: "invalid argument", 2: "CUDA error", 3: "unsupported
 GEOM_TRIANGLE, GEOM_DISK, GEOM_GAUSSIAN = 0, 1, 2
 DOF_AFFINE, DOF_TRIANGLE_MESH = 0, 1
 VOLUME_ONLY, GRADIENT, HESSIAN, ALL = 1, 2, 4, 7
-CONTRACT_FP32, CONTRACT_BF16X3, CONTRACT_TF32X3 = 0, 1, 2
+CONTRACT_FP32, CONTRACT_BF16X3, CONTRACT_TF32X3, CONTRACT_FP16X3 = 0, 1, 2, 3
 
 
 class PointIntError(RuntimeError):

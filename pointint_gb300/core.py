@@ -17,11 +17,11 @@ import numpy as np
 import torch
 
 from . import _lib
-from ._lib import CONTRACT_FP32, CONTRACT_BF16X3, CONTRACT_TF32X3
+from ._lib import CONTRACT_FP32, CONTRACT_BF16X3, CONTRACT_TF32X3, CONTRACT_FP16X3
 from .geometry import SceneObject
 from .kgrid import KGrid
 
-PRECISIONS = {"fp32": CONTRACT_FP32, "bf16x3": CONTRACT_BF16X3, "tf32x3": CONTRACT_TF32X3}
+PRECISIONS = {"fp32": CONTRACT_FP32, "bf16x3": CONTRACT_BF16X3, "tf32x3": CONTRACT_TF32X3, "fp16x3": CONTRACT_FP16X3}
 
 
 def _stream(stream=None) -> ctypes.c_void_p:

@@ -12,8 +12,11 @@
 #include <numeric>
 #include <vector>
 #include "pi_internal.h"
+#include "group.h"
 
 using namespace pi;
+
+constexpr double INV_8PI3 = 1.0 / (8.0 * 3.14159265358979323846 * 3.14159265358979323846 * 3.14159265358979323846);
 
 namespace {
 
@@ -327,7 +330,8 @@ int pi_form_factors(pi_kgrid kg, pi_batch b, int scale_sqrt_w, void* d_J, pi_str
 int pi_contract_workspace_size(pi_kgrid kg, int n, int precision, size_t* bytes) {
   if (!kg || !bytes || n < 0) return fail(PI_ERR_INVALID_ARGUMENT, "pi_contract_workspace_size: bad arguments");
   if (precision == PI_CONTRACT_FP32) *bytes = contract_fp32_ws_bytes(kg->Q, n);
-  else if (precision == PI_CONTRACT_BF16X3) *bytes = contract_tc_ws_bytes(kg->Q, n, 0);
+  else if (precision == PI_CONTRACT_BF16X3) *bytes = group_single_ws_bytes(kg->Q, n, GROUP_OP_BF16);
+  else if (precision == PI_CONTRACT_FP16X3) *bytes = group_single_ws_bytes(kg->Q, n, GROUP_OP_F16);
   else if (precision == PI_CONTRACT_TF32X3) *bytes = contract_tc_ws_bytes(kg->Q, n, 1);
   else return fail(PI_ERR_INVALID_ARGUMENT, "unknown contraction precision");
   return PI_OK;
@@ -339,10 +343,13 @@ int pi_contract(pi_kgrid kg, const void* d_Jw, int n, int precision, double* d_V
   cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
   const float2* J = static_cast<const float2*>(d_Jw);
   if (precision == PI_CONTRACT_FP32) return launch_contract_fp32(kg, J, n, d_V, d_ws, ws_bytes, s);
-  if (precision == PI_CONTRACT_BF16X3 || precision == PI_CONTRACT_TF32X3) {
+  if (precision == PI_CONTRACT_BF16X3 || precision == PI_CONTRACT_TF32X3 || precision == PI_CONTRACT_FP16X3) {
     if (!kg->all_positive)
       return fail(PI_ERR_UNSUPPORTED, "the tensor-core contractions need non-negative quadrature weights");
-    return launch_contract_tc(kg, J, n, precision == PI_CONTRACT_BF16X3 ? 0 : 1, d_V, d_ws, ws_bytes, s);
+    if (precision != PI_CONTRACT_TF32X3)
+      return launch_group_single(J, kg->Q, n, precision == PI_CONTRACT_FP16X3 ? GROUP_OP_F16 : GROUP_OP_BF16, d_V,
+                                 d_ws, ws_bytes, INV_8PI3, s);
+    return launch_contract_tc(kg, J, n, 1, d_V, d_ws, ws_bytes, s);
   }
   return fail(PI_ERR_INVALID_ARGUMENT, "unknown contraction precision");
 }

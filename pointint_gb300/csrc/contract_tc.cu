@@ -28,10 +28,13 @@
 #include <algorithm>
 #include <mutex>
 #include "pi_internal.h"
+#include "tc_ptx.cuh"
 
 namespace pi {
 
 namespace {
+
+using namespace tc;
 
 constexpr int TC_M = 128;                       // tile edge (objects)
 constexpr int TC_STAGES = 3;
@@ -43,7 +46,6 @@ constexpr int TC_THREADS = (TC_PWARPS + 2) * 32;
 constexpr int BLK_BYTES = TC_M * 128;           // 16 KB: one operand block, 128-byte K rows
 constexpr int STAGE_BYTES = 4 * BLK_BYTES;      // A hi, A lo, B hi, B lo
 constexpr int SMEM_BYTES = TC_STAGES * STAGE_BYTES + 1024;  // + alignment slack
-constexpr long long WAIT_CYCLES = 4000000000LL; // ~2 s at 2 GHz
 constexpr double INV8PI3 = 1.0 / (8.0 * 3.14159265358979323846 * 3.14159265358979323846 * 3.14159265358979323846);
 
 // Operand kinds.  A 128-byte K row holds 64 BF16 or 32 TF32 values; each
@@ -57,176 +59,22 @@ template <> struct Kind<KIND_TF32> { static constexpr int EPC = 4; static conste
 // B format at bits 7-9 / 10-12 (1 = BF16, 2 = TF32), both K-major, N >> 3 at
 // bits 17-22, M >> 4 at bits 24-28.
 template <int KIND>
-constexpr uint32_t idesc() {
-  return (1u << 4) | (Kind<KIND>::FMT << 7) | (Kind<KIND>::FMT << 10) | ((uint32_t)(TC_M >> 3) << 17) |
-         ((uint32_t)(TC_M >> 4) << 24);
-}
+__host__ __device__ constexpr uint32_t idesc() { return tc::idesc(Kind<KIND>::FMT, TC_M, TC_M); }
 
 enum { ERR_PRODUCER_WAIT = 1, ERR_MMA_WAIT = 2, ERR_EPILOGUE_WAIT = 3, ERR_TMA_WAIT = 4 };
 
-__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
-
-__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
-}
-
-__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
-  asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.shared::cta.b64 st, [%0];\n\t}" ::"r"(bar) : "memory");
-}
-
-__device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
-  uint32_t ok;
-  asm volatile(
-      "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
-      : "=r"(ok)
-      : "r"(bar), "r"(parity)
-      : "memory");
-  return ok != 0;
-}
-
-// Bounded wait for the completion of the barrier phase with the given parity.
-// Returns false (after recording `code`) on expiry, or at once if another
-// thread of the grid has already recorded an error.
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, int* err, int code) {
-  const long long t0 = clock64();
-  while (!mbar_try_wait(bar, parity)) {
-    if (*reinterpret_cast<volatile int*>(err) != 0) return false;
-    if (clock64() - t0 > WAIT_CYCLES) {
-      atomicCAS(err, 0, code);
-      return false;
-    }
-  }
-  return true;
-}
-
-__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
-  asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.expect_tx.shared::cta.b64 st, [%0], %1;\n\t}" ::"r"(bar),
-               "r"(bytes)
-               : "memory");
-}
-
-// 2D tiled TMA load of a box of FP32 J (x = K coordinate, a multiple of 4
-// elements = 16 bytes; y = row) into shared memory, completing on `bar`.
-__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map, int x, int y, uint32_t bar) {
-  asm volatile(
-      "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::
-          "r"(dst),
-      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(bar)
-      : "memory");
-}
-
-// Bounded wait used only to drain copies already in flight; ignores the flag.
-__device__ __forceinline__ void mbar_drain(uint32_t bar, uint32_t parity) {
-  const long long t0 = clock64();
-  while (!mbar_try_wait(bar, parity) && clock64() - t0 <= WAIT_CYCLES) {
-  }
-}
-
-// Named barrier 1 over the converter warps with an OR-reduction, so every
-// converter takes the same exit decision.
-__device__ __forceinline__ bool converters_any(bool pred) {
-  uint32_t r;
-  asm volatile(
-      "{\n\t.reg .pred p, q;\n\tsetp.ne.b32 q, %1, 0;\n\tbar.red.or.pred p, 1, %2, q;\n\tselp.u32 %0, 1, 0, p;\n\t}"
-      : "=r"(r)
-      : "r"((uint32_t)pred), "r"(TC_PWARPS * 32)
-      : "memory");
-  return r != 0;
-}
-
-__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
-__device__ __forceinline__ void fence_mbar_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
-__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
-__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
-
-// Shared-memory matrix descriptor, K-major, 128-byte swizzle: start address
-// (>>4, bits 0-13), leading byte offset (unused for this layout, 16 B),
-// stride byte offset 1024 B between 8-row swizzle atoms (bits 32-45),
-// descriptor version 1 (bits 46-48), swizzle mode 2 = 128 B (bits 61-63).
-__device__ __forceinline__ uint64_t desc_sw128(uint32_t saddr) {
-  uint64_t d = (uint64_t)((saddr & 0x3FFFFu) >> 4);
-  d |= (uint64_t)1 << 16;
-  d |= (uint64_t)(1024 >> 4) << 32;
-  d |= (uint64_t)1 << 46;
-  d |= (uint64_t)2 << 61;
-  return d;
-}
-
 template <int KIND>
 __device__ __forceinline__ void umma(uint32_t tmem_d, uint64_t a, uint64_t b, uint32_t accumulate) {
-  if (KIND == KIND_BF16) {
-    asm volatile(
-        "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %3, 0;\n\t"
-        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %4, p;\n\t}" ::"r"(tmem_d),
-        "l"(a), "l"(b), "r"(accumulate), "r"(idesc<KIND_BF16>())
-        : "memory");
-  } else {
-    asm volatile(
-        "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %3, 0;\n\t"
-        "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %4, p;\n\t}" ::"r"(tmem_d),
-        "l"(a), "l"(b), "r"(accumulate), "r"(idesc<KIND_TF32>())
-        : "memory");
-  }
+  if (KIND == KIND_BF16) umma_f16(tmem_d, a, b, idesc<KIND_BF16>(), accumulate);
+  else umma_tf32(tmem_d, a, b, idesc<KIND_TF32>(), accumulate);
 }
 
-__device__ __forceinline__ void umma_commit(uint32_t bar) {
-  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
-}
-
-__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float* v) {
-  uint32_t r[32];
-  asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, "
-      "%16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
-      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
-        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]),
-        "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
-        "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
-      : "r"(taddr));
-  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-  for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
-}
+__device__ __forceinline__ bool converters_any(bool pred) { return bar_any(1, TC_PWARPS * 32, pred); }
 
 __device__ __forceinline__ void tile_of(int p, int nt, int* bi, int* bj) {
   int i = 0, rem = p;
   while (rem >= nt - i) { rem -= nt - i; ++i; }
   *bi = i; *bj = i + rem;
-}
-
-__device__ __forceinline__ uint32_t pack_bf16(float a, float b) {
-  __nv_bfloat162 v = __floats2bfloat162_rn(a, b);
-  return *reinterpret_cast<uint32_t*>(&v);
-}
-
-__device__ __forceinline__ float to_tf32(float x) {  // round to nearest TF32, kept as an FP32 bit pattern
-  uint32_t r;
-  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
-  return __uint_as_float(r);
-}
-
-// Split 4 consecutive FP32 values into TF32 hi / lo halves (16 B each).
-__device__ __forceinline__ void split4_tf32(const float* x, uint4* hi, uint4* lo) {
-  float h[4], l[4];
-#pragma unroll
-  for (int i = 0; i < 4; ++i) {
-    h[i] = to_tf32(x[i]);
-    l[i] = to_tf32(x[i] - h[i]);
-  }
-  *hi = make_uint4(__float_as_uint(h[0]), __float_as_uint(h[1]), __float_as_uint(h[2]), __float_as_uint(h[3]));
-  *lo = make_uint4(__float_as_uint(l[0]), __float_as_uint(l[1]), __float_as_uint(l[2]), __float_as_uint(l[3]));
-}
-
-// Split 8 consecutive FP32 values into bf16 hi / lo halves (16 B each).
-__device__ __forceinline__ void split8(const float* x, uint4* hi, uint4* lo) {
-  float h[8], l[8];
-#pragma unroll
-  for (int i = 0; i < 8; ++i) {
-    h[i] = __bfloat162float(__float2bfloat16_rn(x[i]));
-    l[i] = x[i] - h[i];
-  }
-  *hi = make_uint4(pack_bf16(h[0], h[1]), pack_bf16(h[2], h[3]), pack_bf16(h[4], h[5]), pack_bf16(h[6], h[7]));
-  *lo = make_uint4(pack_bf16(l[0], l[1]), pack_bf16(l[2], l[3]), pack_bf16(l[4], l[5]), pack_bf16(l[6], l[7]));
 }
 
 template <int KIND>
@@ -258,14 +106,13 @@ syrk_split3_kernel(const __grid_constant__ CUtensorMap xmap, int n, int64_t K, i
     fence_mbar_init();
   }
   if (warp == TC_MMA_WARP) {
-    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_slot)),
-                 "r"(TC_M));
-    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    tmem_alloc(smem_u32(&tmem_slot), 2 * TC_M);
   }
-  tc_fence_before();
+  fence_before();
   __syncthreads();
-  tc_fence_after();
-  const uint32_t tmem = tmem_slot;
+  fence_after();
+  const uint32_t tmem = tmem_slot;          // main accumulator (hi.hi)
+  const uint32_t tmem_c = tmem + TC_M;      // correction accumulator (hi.lo + lo.hi)
 
   constexpr int EPC = Kind<KIND>::EPC;
   constexpr int KC = 8 * EPC;                              // K elements per stage
@@ -348,7 +195,7 @@ syrk_split3_kernel(const __grid_constant__ CUtensorMap xmap, int n, int64_t K, i
       const int s = (int)(c % TC_STAGES);
       const int64_t r = c / TC_STAGES;
       if (!mbar_wait(smem_u32(&full_bar[s]), (uint32_t)(r & 1), err, ERR_MMA_WAIT)) break;
-      tc_fence_after();
+      fence_after();
       const uint32_t st = smem_u32(smem + s * STAGE_BYTES);
       const uint64_t aH = desc_sw128(st), aL = desc_sw128(st + BLK_BYTES);
       const uint64_t bH = diag ? aH : desc_sw128(st + 2 * BLK_BYTES);
@@ -356,9 +203,10 @@ syrk_split3_kernel(const __grid_constant__ CUtensorMap xmap, int n, int64_t K, i
 #pragma unroll
       for (int k = 0; k < 4; ++k) {  // one MMA covers 32 bytes of K (16 BF16 / 8 TF32)
         const uint64_t adv = (uint64_t)(k * 32) >> 4;  // +32 bytes along K inside the swizzled row
-        umma<KIND>(tmem, aH + adv, bH + adv, (c > 0 || k > 0) ? 1u : 0u);
-        umma<KIND>(tmem, aH + adv, bL + adv, 1u);
-        umma<KIND>(tmem, aL + adv, bH + adv, 1u);
+        const uint32_t acc = (c > 0 || k > 0) ? 1u : 0u;
+        umma<KIND>(tmem, aH + adv, bH + adv, acc);
+        umma<KIND>(tmem_c, aH + adv, bL + adv, acc);
+        umma<KIND>(tmem_c, aL + adv, bH + adv, 1u);
       }
       umma_commit(smem_u32(&empty_bar[s]));
     }
@@ -368,14 +216,18 @@ syrk_split3_kernel(const __grid_constant__ CUtensorMap xmap, int n, int64_t K, i
   // ---------------- epilogue: TMEM -> FP32 partial tile ----------------
   if (warp < 4) {
     const bool ok = mbar_wait(smem_u32(&done_bar), 0u, err, ERR_EPILOGUE_WAIT);
-    tc_fence_after();
+    fence_after();
     const int row = warp * 32 + lane;
     float* out = partials + ((int64_t)blockIdx.y * gridDim.x + blockIdx.x) * (TC_M * TC_M) + (int64_t)row * TC_M;
 #pragma unroll 1
     for (int cb = 0; cb < TC_M / 32; ++cb) {
       float v[32];
       if (ok && nc > 0) {
+        float cc[32];
         tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(cb * 32), v);
+        tmem_ld32(tmem_c + ((uint32_t)(warp * 32) << 16) + (uint32_t)(cb * 32), cc);
+#pragma unroll
+        for (int i = 0; i < 32; ++i) v[i] += cc[i];
       } else {
 #pragma unroll
         for (int i = 0; i < 32; ++i) v[i] = 0.f;
@@ -385,12 +237,12 @@ syrk_split3_kernel(const __grid_constant__ CUtensorMap xmap, int n, int64_t K, i
         *reinterpret_cast<float4*>(out + cb * 32 + i) = make_float4(v[i], v[i + 1], v[i + 2], v[i + 3]);
     }
   }
-  tc_fence_before();
+  fence_before();
   __syncthreads();
   if (warp == TC_MMA_WARP) {
     __syncwarp();
-    tc_fence_after();
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TC_M));
+    fence_after();
+    tmem_dealloc(tmem, 2 * TC_M);
   }
 }
 

@@ -69,6 +69,17 @@ __device__ __forceinline__ df cdot(float3 dh, float3 dl, float3 x) {
   return quick_two_sum(t.hi, lo);
 }
 
+// (dh + dl) . (xh + xl) in double-float; the dl . xl term (~2^-48 relative)
+// is dropped.
+__device__ __forceinline__ df cdot2(float3 dh, float3 dl, float3 xh, float3 xl) {
+  df p0 = two_prod(dh.x, xh.x), p1 = two_prod(dh.y, xh.y), p2 = two_prod(dh.z, xh.z);
+  df s = two_sum(p0.hi, p1.hi);
+  df t = two_sum(s.hi, p2.hi);
+  float lo = s.lo + t.lo + p0.lo + p1.lo + p2.lo + (dl.x * xh.x + dl.y * xh.y + dl.z * xh.z) +
+             (dh.x * xl.x + dh.y * xl.y + dh.z * xl.z);
+  return quick_two_sum(t.hi, lo);
+}
+
 // pi/2 = 1.57079632679489661923132169163975144209858...
 //   PIO2_A = FP32(pi/2)            = 1.5707963705062866
 //   PIO2_B = FP32(pi/2 - PIO2_A)   = -4.371138828673793e-08
@@ -86,20 +97,41 @@ struct cf { float re, im; };
 // fitted on Chebyshev-spaced samples of [-pi/4, pi/4]; FP32 evaluation error
 // <= 7e-8 each, about 5x below the hardware sin/cos approximation.  The
 // quadrant n mod 4 rotates the result.
-__device__ __forceinline__ cf cis(df x) {
-  const float n = rintf(x.hi * PI_TWO_OVER_PI);
-  float r = fmaf(-n, PI_PIO2_A, x.hi);
-  r = fmaf(-n, PI_PIO2_B, r);
-  r += x.lo;
+// e^{i (r + q pi/2)} for r in [-pi/4, pi/4]: this project's own least-squares
+// polynomials for sin(r)/r (degree 4 in r^2) and cos(r) (degree 5 in r^2),
+// fitted on Chebyshev-spaced samples of [-pi/4, pi/4]; FP32 evaluation error
+// <= 7e-8 each, about 5x below the hardware sin/cos approximation.  The
+// quadrant q mod 4 rotates the result.
+__device__ __forceinline__ cf cis_quadrant(float r, int q) {
   const float t = r * r;
   const float sn = r * fmaf(t, fmaf(t, fmaf(t, fmaf(t, 2.717349162e-06f, -1.983920229e-04f), 8.333329111e-03f),
                                      -1.666666716e-01f), 1.0f);
   const float cs = fmaf(t, fmaf(t, fmaf(t, fmaf(t, fmaf(t, -2.717345637e-07f, 2.479892828e-05f), -1.388887991e-03f),
                                       4.166666791e-02f), -0.5f), 1.0f);
-  const int q = __float2int_rn(n) & 3;
+  q &= 3;
   const float s1 = (q & 1) ? cs : sn;   // sin(r + q pi/2) up to sign
   const float c1 = (q & 1) ? sn : cs;   // cos(r + q pi/2) up to sign
   return {((q + 1) & 2) ? -c1 : c1, (q & 2) ? -s1 : s1};
+}
+
+// e^{i x} for a double-float phase x (|x| < ~1e5): Cody-Waite reduction by
+// pi/2 to r in [-pi/4, pi/4] (fmaf(-n, A, x) is exact: the result needs at
+// most 23 significant bits), then cis_quadrant.
+__device__ __forceinline__ cf cis(df x) {
+  const float n = rintf(x.hi * PI_TWO_OVER_PI);
+  float r = fmaf(-n, PI_PIO2_A, x.hi);
+  r = fmaf(-n, PI_PIO2_B, r);
+  r += x.lo;
+  return cis_quadrant(r, __float2int_rn(n));
+}
+
+// e^{2 pi i t} for a phase given in turns, |t| < 2^20: the nearest quarter
+// turn n/4 is removed exactly (t - n/4 needs no more bits than t), and
+// r = 2 pi (t - n/4) lies in [-pi/4, pi/4] up to rounding.
+__device__ __forceinline__ cf cis_turns(float t) {
+  const float n = rintf(4.0f * t);
+  const float r = fmaf(-0.25f, n, t) * 6.283185307179586f;
+  return cis_quadrant(r, __float2int_rn(n));
 }
 
 __device__ __forceinline__ cf cmul(cf a, cf b) { return {a.re * b.re - a.im * b.im, a.re * b.im + a.im * b.re}; }

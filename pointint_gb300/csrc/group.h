@@ -1,0 +1,113 @@
+// Grouped volume contraction: many independent volume matrices (one per
+// query) in one persistent launch.
+//
+// Every query is a list of operand rows.  A row is one object's sqrt|w|-scaled
+// form factors J (ncols complex values), optionally the maximum |x| over the
+// row's real and imaginary parts (which sets the power-of-two scale of the
+// FP16 split), and a translation c whose phase e^{i k.c} is applied as the row
+// is staged (direction-major rows only).  A query with n rows owns the
+// upper-triangle pairs of its 128-row tiles; each pair is cut along k into
+// nsplit work items, item s taking the chunks (32 complex columns each)
+// s, s + nsplit, s + 2 nsplit, ...  Items are ordered split-major, so CTAs
+// running at the same time read the same chunks of a tile (one DRAM read, the
+// other pairs hit L2) and neighbouring chunks of each row (long DRAM runs).
+// Each work item writes a 128 x 128 FP32 partial tile, and the reduction sums
+// the partials of every pair in a fixed order in FP64: a query's result does
+// not depend on which other queries share the launch.
+//
+// All counts live in device memory (GHeader), so a launch sequence captured
+// once in a CUDA graph serves every batch.
+#pragma once
+#include <cuda.h>
+#include <cuda_runtime.h>
+#include <cstdint>
+
+namespace pi {
+
+constexpr int GROUP_TILE = 128;        // rows per tile
+constexpr int GROUP_CHUNK = 32;        // complex columns per k chunk
+constexpr int GROUP_MAX_L = 512;       // radial nodes per direction supported by the phase path
+
+enum { GROUP_OP_BF16 = 0, GROUP_OP_F16 = 1 };
+
+struct GRow {                          // 40 bytes
+  const float2* J;                     // ncols complex values, 16-byte aligned
+  const float* amax;                   // max |Re|, |Im| over the row (FP16 operands), or null
+  float c_hi[3], c_lo[3];              // translation c = c_hi + c_lo
+};
+
+struct GItem {                         // 32 bytes
+  int32_t row_a, row_b;                // first row of each tile (absolute row index)
+  int32_t na, nb;                      // valid rows in each tile (1..128)
+  int32_t chunk0, nchunks;             // k chunks chunk0 + c * cstride, c < nchunks
+  int32_t cstride;                     // = the query's nsplit: the splits of a pair interleave, so the
+                                       // CTAs running at one time read neighbouring chunks of each row
+  int32_t query;
+};
+
+struct GQuery {                        // 32 bytes
+  int32_t row0, n;                     // rows [row0, row0 + n)
+  int32_t nt, nsplit;                  // tiles, k splits per tile pair
+  int64_t item0;                       // first work item; item0 + split * npairs + pair
+  int64_t out_off;                     // V (n x n, FP64) at out + out_off
+};
+
+struct GHeader {                       // 16 bytes
+  int32_t n_items, n_queries;
+  int64_t n_elems;                     // sum of n^2 over queries
+};
+
+struct GroupDev {                      // kernel argument; pointers fixed for the life of a graph
+  const GHeader* hdr;
+  const GRow* rows;
+  const GItem* items;
+  const GQuery* queries;
+  const int64_t* elem0;                // per query: prefix sum of n^2
+  int64_t ncols;                       // complex columns per row
+  int32_t op;                          // GROUP_OP_*
+  int32_t phase;                       // 1: rows are direction-major (col = j * L + r) and get e^{i k.c}
+  int32_t L, M;                        // radial nodes per direction, directions
+  const float4* dir_hi;                // directions (double-float), M entries
+  const float4* dir_lo;
+  const float2* kturn;                 // kmag / 2 pi (double-float), L entries
+  float* partials;                     // n_items x 128 x 128
+  int* err;                            // 0 = ok
+  double* out;                         // output arena
+  double scale;                        // 1 / (8 pi^3)
+};
+
+// Power-of-two operand scale of a row with maximum |x| = amax: the scaled
+// maximum lies in [2^14, 2^15), inside FP16's range with its full precision.
+__host__ __device__ inline float group_row_scale(float amax) {
+  if (!(amax > 0.f) || !(amax < 3.0e38f)) return 1.f;
+  int e;
+  (void)frexpf(amax, &e);  // amax = m 2^e, m in [0.5, 1)
+  return ldexpf(1.f, 15 - e);
+}
+
+size_t group_smem_bytes();
+int group_threads();
+int group_grid();                      // persistent grid on the current device
+const void* group_contract_fn(int op, int phase, int tma);
+const void* group_reduce_fn();
+int group_reduce_threads();
+int group_prepare_attributes();
+
+// 2D tensor map over n_rows contiguous rows of row_floats FP32 values, in the
+// contraction's 128-row x 32-value boxes, 128-byte swizzled.
+int encode_row_map(CUtensorMap* map, const void* base, int64_t row_floats, int64_t n_rows);
+
+// Direct launches (not captured).  xmap != null selects the TMA loader (rows
+// of g.items are then row coordinates of the map); null the cp.async gather
+// through g.rows[].J.
+int launch_group_contract(const GroupDev& g, const CUtensorMap* xmap, int grid, cudaStream_t s);
+int launch_group_reduce(const GroupDev& g, int grid, cudaStream_t s);
+
+// One query over n contiguous rows Jw + i * Q (the pi_contract layout): the
+// descriptors (and, for FP16 operands, the row maxima) are formed on the
+// device inside the workspace.
+size_t group_single_ws_bytes(int64_t Q, int n, int op);
+int launch_group_single(const float2* Jw, int64_t Q, int n, int op, double* V, void* ws, size_t ws_bytes,
+                        double scale, cudaStream_t s);
+
+}  // namespace pi
