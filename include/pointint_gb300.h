@@ -237,6 +237,76 @@ int pi_compute_Ak(const pi_object* obj, const double* dirs, const double* kmag, 
  * k-vector, host in and out (out = re, im). */
 int pi_compute_Ak_single(const pi_object* obj, const double* k, double* out);
 
+/* ---- serving: resident form factors, rigid-transform queries ----------------
+ * No reference counterpart: the reference evaluates every object's form
+ * factors from scratch on every call (compute_intersection_volume_multi_object.cu:234-713).
+ *
+ * A server owns a library of objects (elements + DoFs, uploaded once) and a
+ * pool of resident form-factor rows in HBM.  A query is a scene: a list of
+ * library objects, each under a rigid transform x' = R x + t applied on top of
+ * its DoFs; the result is the scene's volume matrix (n x n, FP64, 1/(8 pi^3)
+ * applied).  Translations never re-evaluate form factors: the phase
+ * e^{i k . c} of each object's centre c = R o + t is applied inside the
+ * contraction.  A rotation evaluates the object's form factors at R^T k into a
+ * row owned by that query.  A worker thread admits pending queries, in arrival
+ * order, into up to `inflight_batches` batches on the device at once, as long
+ * as the resident pool (LRU, within hbm_budget_bytes) and the batch arenas have
+ * room; each batch runs as one CUDA graph (descriptor upload, form factors of
+ * the new rows, one persistent tensor-core contraction over every query of the
+ * batch, the FP64 reduction, result download).  Each query's result depends on
+ * that query alone, not on the batch it ran in. */
+typedef struct pi_server_s* pi_server;
+
+typedef struct {
+  int64_t hbm_budget_bytes;  /* resident rows + batch arenas; 0 = a quarter of the free device memory */
+  int32_t max_batch_queries; /* 0 = 64 */
+  int32_t max_batch_rows;    /* object rows (sum of n over the batch's queries); 0 = 4096 */
+  int32_t max_batch_evals;   /* form-factor evaluations per batch; 0 = 256 */
+  int32_t inflight_batches;  /* 1..4; 0 = 2 */
+  int32_t precision;         /* PI_CONTRACT_FP16X3 (0 = default) or PI_CONTRACT_BF16X3 */
+  int32_t use_graphs;        /* 1: each batch is one CUDA graph launch; 0: plain stream launches; -1 = 1 */
+  int32_t autotune;          /* 1: time work-item sizes at creation; 0: built-in sizes; -1 = 1 */
+  int32_t reserved_;
+} pi_server_config;
+
+typedef struct {
+  int32_t n_objects;         /* rows of the scene (a library object may appear more than once) */
+  int32_t reserved_;
+  const int32_t* objects;    /* library indices */
+  const double* rotations;   /* n x 9 row-major proper rotations, or NULL (no rotation) */
+  const double* translations;/* n x 3, or NULL (no translation) */
+} pi_query;
+
+enum { PI_QUERY_PENDING = 0, PI_QUERY_RUNNING = 1, PI_QUERY_DONE = 2, PI_QUERY_FAILED = 3, PI_QUERY_CANCELLED = 4 };
+
+typedef struct {
+  int64_t submitted, completed, failed, cancelled;
+  int64_t batches, evaluations, resident_hits, resident_misses, evictions;
+  int64_t pool_rows, resident_rows, graph_launches;
+  int32_t tuned_items_per_sm[4];  /* autotuned work items per SM for scenes of <= 16, <= 128, <= 512, > 512 objects, x 1/4 */
+} pi_server_stats;
+
+/* Zero config fields take the defaults above. */
+int pi_server_create(pi_kgrid kg, const pi_object* library, int n_library, const pi_server_config* cfg,
+                     pi_server* out);
+/* Queue a scene.  V_out (host, n x n row-major) is written before the ticket
+ * reads as done; it must stay valid until then. */
+int pi_server_submit(pi_server s, const pi_query* q, double* V_out, uint64_t* ticket);
+int pi_server_poll(pi_server s, uint64_t ticket, int32_t* state);
+/* Block until the ticket is done (PI_OK), failed (its error), cancelled, or
+ * timeout_s elapses (PI_ERR_TIMEOUT; timeout_s < 0 waits forever). */
+int pi_server_wait(pi_server s, uint64_t ticket, double timeout_s);
+/* Cancels a query that has not been admitted to a batch yet (PI_OK); a
+ * running or finished query is left alone (PI_ERR_UNSUPPORTED). */
+int pi_server_cancel(pi_server s, uint64_t ticket);
+/* Host steady-clock nanoseconds: submitted, admitted to a batch, result written. */
+int pi_server_times(pi_server s, uint64_t ticket, int64_t* submit_ns, int64_t* start_ns, int64_t* done_ns);
+/* Forget a finished ticket. */
+int pi_server_release(pi_server s, uint64_t ticket);
+int pi_server_stats_get(pi_server s, pi_server_stats* st);
+/* Waits for the queries already admitted, fails the pending ones, frees everything. */
+int pi_server_destroy(pi_server s);
+
 #ifdef __cplusplus
 }
 #endif

@@ -38,6 +38,29 @@ class PiObject(ctypes.Structure):
                 ("n_dofs", ctypes.c_int64), ("dofs", ctypes.c_void_p)]
 
 
+class ServerConfig(ctypes.Structure):
+    """pi_server_config (zero fields take the library's defaults)."""
+    _fields_ = [("hbm_budget_bytes", ctypes.c_int64), ("max_batch_queries", ctypes.c_int32),
+                ("max_batch_rows", ctypes.c_int32), ("max_batch_evals", ctypes.c_int32),
+                ("inflight_batches", ctypes.c_int32), ("precision", ctypes.c_int32),
+                ("use_graphs", ctypes.c_int32), ("autotune", ctypes.c_int32), ("reserved_", ctypes.c_int32)]
+
+
+class Query(ctypes.Structure):
+    """pi_query: library indices + optional per-object rotations (n x 9) and translations (n x 3)."""
+    _fields_ = [("n_objects", ctypes.c_int32), ("reserved_", ctypes.c_int32), ("objects", ctypes.c_void_p),
+                ("rotations", ctypes.c_void_p), ("translations", ctypes.c_void_p)]
+
+
+class ServerStats(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_int64) for n in ("submitted", "completed", "failed", "cancelled", "batches",
+                                             "evaluations", "resident_hits", "resident_misses", "evictions",
+                                             "pool_rows", "resident_rows", "graph_launches")] + \
+               [("tuned_items_per_sm", ctypes.c_int32 * 4)]
+
+
+QUERY_PENDING, QUERY_RUNNING, QUERY_DONE, QUERY_FAILED, QUERY_CANCELLED = 0, 1, 2, 3, 4
+
 _lock = threading.Lock()
 _lib = None
 
@@ -87,6 +110,15 @@ SIGNATURES = {
     "pi_pair_volume_host": (I32, [OBJP, OBJP, P, P, P, I64, ctypes.POINTER(D)]),
     "pi_compute_Ak": (I32, [OBJP, P, P, I64, P, I32]),
     "pi_compute_Ak_single": (I32, [OBJP, P, P]),
+    "pi_server_create": (I32, [P, OBJP, I32, ctypes.POINTER(ServerConfig), PP]),
+    "pi_server_submit": (I32, [P, ctypes.POINTER(Query), P, ctypes.POINTER(ctypes.c_uint64)]),
+    "pi_server_poll": (I32, [P, ctypes.c_uint64, ctypes.POINTER(ctypes.c_int32)]),
+    "pi_server_wait": (I32, [P, ctypes.c_uint64, D]),
+    "pi_server_cancel": (I32, [P, ctypes.c_uint64]),
+    "pi_server_times": (I32, [P, ctypes.c_uint64, ctypes.POINTER(I64), ctypes.POINTER(I64), ctypes.POINTER(I64)]),
+    "pi_server_release": (I32, [P, ctypes.c_uint64]),
+    "pi_server_stats_get": (I32, [P, ctypes.POINTER(ServerStats)]),
+    "pi_server_destroy": (I32, [P]),
 }
 
 

@@ -20,7 +20,8 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libpointint_gb300.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["host.cpp", "capi.cu", "formfactor.cu", "contract.cu", "contract_tc.cu", "contract_group.cu", "adjoint.cu"]
+SOURCES = ["host.cpp", "capi.cu", "formfactor.cu", "contract.cu", "contract_tc.cu", "contract_group.cu", "adjoint.cu",
+           "server.cpp"]
 
 
 def nvcc() -> str:

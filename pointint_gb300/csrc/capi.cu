@@ -144,7 +144,7 @@ int pi_kgrid_create(const double* dirs, const double* kmag, const double* w, int
   const int64_t L = tensor ? Q / M : 1;
   if (!tensor) M = Q;
   std::vector<float4> dh(M), dl(M);
-  std::vector<float2> km(L);
+  std::vector<float2> km(L), kt(L);
   for (int64_t j = 0; j < M; ++j) {
     double d[3];
     for (int c = 0; c < 3; ++c) d[c] = tensor ? dirs[3 * j + c] : dirs[3 * j + c] * kmag[j];
@@ -158,6 +158,9 @@ int pi_kgrid_create(const double* dirs, const double* kmag, const double* w, int
     const double k = tensor ? kmag[r * M] : 1.0;
     const float h = (float)k;
     km[r] = make_float2(h, (float)(k - (double)h));
+    const double u = k / (2.0 * 3.14159265358979323846);
+    const float uh = (float)u;
+    kt[r] = make_float2(uh, (float)(u - (double)uh));
   }
   std::vector<float> sw(Q), sg(Q);
   kg->w.resize(Q);
@@ -171,13 +174,14 @@ int pi_kgrid_create(const double* dirs, const double* kmag, const double* w, int
   }
   const size_t o_dh = 0, o_dl = align16(o_dh + M * sizeof(float4)), o_km = align16(o_dl + M * sizeof(float4)),
                o_sw = align16(o_km + L * sizeof(float2)), o_sg = align16(o_sw + Q * sizeof(float)),
-               total = align16(o_sg + Q * sizeof(float));
+               o_kt = align16(o_sg + Q * sizeof(float)), total = align16(o_kt + L * sizeof(float2));
   std::vector<unsigned char> host(total, 0);
   std::memcpy(host.data() + o_dh, dh.data(), M * sizeof(float4));
   std::memcpy(host.data() + o_dl, dl.data(), M * sizeof(float4));
   std::memcpy(host.data() + o_km, km.data(), L * sizeof(float2));
   std::memcpy(host.data() + o_sw, sw.data(), Q * sizeof(float));
   std::memcpy(host.data() + o_sg, sg.data(), Q * sizeof(float));
+  std::memcpy(host.data() + o_kt, kt.data(), L * sizeof(float2));
   PI_CUDA(cudaMalloc(&kg->d_mem, total));
   cudaError_t e = cudaMemcpy(kg->d_mem, host.data(), total, cudaMemcpyHostToDevice);
   if (e != cudaSuccess) { cudaFree(kg->d_mem); return cuda_fail(e, "pi_kgrid_create upload"); }
@@ -189,6 +193,7 @@ int pi_kgrid_create(const double* dirs, const double* kmag, const double* w, int
   kg->dev.kmag = reinterpret_cast<const float2*>(base + o_km);
   kg->dev.sqrtw = reinterpret_cast<const float*>(base + o_sw);
   kg->dev.sign = reinterpret_cast<const float*>(base + o_sg);
+  kg->dev.kturn = reinterpret_cast<const float2*>(base + o_kt);
   *out = kg.release();
   return PI_OK;
 }

@@ -82,7 +82,7 @@ __device__ __forceinline__ uint32_t stage_off(int r, int u) {
 // kind::f16 operand format: 0 = F16, 1 = BF16.
 template <int OP> constexpr uint32_t op_idesc() { return idesc(OP == GROUP_OP_F16 ? 0u : 1u, GM, GM); }
 
-enum { ERR_LOAD = 1, ERR_CONVERT = 2, ERR_MMA = 3, ERR_EPILOGUE = 4 };
+enum { ERR_LOAD = 1, ERR_CONVERT = 2, ERR_MMA = 3, ERR_EPILOGUE = 4, ERR_CAPACITY = 5 };
 
 // x[0..31] = 16 complex values of one row, columns col0 .. col0 + 15 of a
 // direction-major row (col = j L + r).  Multiplies them by e^{2 pi i kturn_r (d_j . c)}.
@@ -149,8 +149,12 @@ group_split3_kernel(const GroupDev g, const __grid_constant__ CUtensorMap xmap) 
 
   uint8_t* smem = smem_raw + ((1024 - (smem_u32(smem_raw) & 1023)) & 1023);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int n_items = g.hdr->n_items;
   int* err = g.err;
+  int n_items = g.hdr->n_items;
+  if (n_items > g.max_items) {  // descriptor inconsistent with the partial arena: do no work
+    if (threadIdx.x == 0 && blockIdx.x == 0) atomicCAS(err, 0, ERR_CAPACITY);
+    n_items = 0;
+  }
 
   if (tid == 0) {
     for (int s = 0; s < NST; ++s) {
@@ -181,7 +185,7 @@ group_split3_kernel(const GroupDev g, const __grid_constant__ CUtensorMap xmap) 
     if (TMA) {
       if (box == 0 && lane == 0) {
         for (int it = blockIdx.x; it < n_items && ok; it += gridDim.x) {
-          const GItem w = g.items[it];
+          const GItem w = group_item(g, it);
           const bool diag = w.row_a == w.row_b;
           for (int c = 0; c < w.nchunks; ++c, ++gc) {
             const int s = (int)(gc % NST);
@@ -208,7 +212,7 @@ group_split3_kernel(const GroupDev g, const __grid_constant__ CUtensorMap xmap) 
     } else {
       const int piece = lane & 15, rpar = lane >> 4;
       for (int it = blockIdx.x; it < n_items && ok; it += gridDim.x) {
-        const GItem w = g.items[it];
+        const GItem w = group_item(g, it);
         const bool diag = w.row_a == w.row_b;
         const int nrows = box == 0 ? w.na : (diag ? 0 : w.nb);
         const int rbase = box == 0 ? w.row_a : w.row_b;
@@ -259,7 +263,7 @@ group_split3_kernel(const GroupDev g, const __grid_constant__ CUtensorMap xmap) 
     int64_t gc = 0;
     bool ok = true;
     for (int it = blockIdx.x; it < n_items && ok; it += gridDim.x) {
-      const GItem w = g.items[it];
+      const GItem w = group_item(g, it);
       const bool diag = w.row_a == w.row_b;
       const bool va = row < w.na, vb = !diag && row < w.nb;
       float3 cah = make_float3(0.f, 0.f, 0.f), cal = cah, cbh = cah, cbl = cah;
@@ -326,7 +330,7 @@ group_split3_kernel(const GroupDev g, const __grid_constant__ CUtensorMap xmap) 
       int64_t gc = 0, gch = 0;
       bool ok = true;
       for (int it = blockIdx.x; it < n_items && ok; it += gridDim.x) {
-        const GItem w = g.items[it];
+        const GItem w = group_item(g, it);
         const bool diag = w.row_a == w.row_b;
         for (int c = 0; c < w.nchunks; ++c, ++gc) {
           const int b = (int)(gch & 1);
@@ -370,7 +374,7 @@ group_split3_kernel(const GroupDev g, const __grid_constant__ CUtensorMap xmap) 
     int64_t gch = 0;
     bool ok = true;
     for (int it = blockIdx.x; it < n_items && ok; it += gridDim.x) {
-      const GItem w = g.items[it];
+      const GItem w = group_item(g, it);
       const int nch = (w.nchunks + CHAIN - 1) / CHAIN;
       const int ncb = (w.nb + 31) >> 5;
       float* out = g.partials + (int64_t)it * (GM * GM) + (int64_t)row * GM;
@@ -434,11 +438,13 @@ __global__ void __launch_bounds__(RED_THREADS) group_reduce_kernel(const GroupDe
     const int npairs = q.nt * (q.nt + 1) / 2;
     const int p = ta * q.nt - ta * (ta - 1) / 2 + (tb - ta);
     const int64_t off = (int64_t)(i % GM) * GM + (j % GM);
-    double s = 0.0;
-    for (int sp = 0; sp < q.nsplit; ++sp)
-      s += (double)g.partials[(q.item0 + (int64_t)sp * npairs + p) * (GM * GM) + off];
-    const double unscale = 1.0 / ((double)row_scale(g.rows[q.row0 + i], g.op) * (double)row_scale(g.rows[q.row0 + j], g.op));
-    s = bad ? __longlong_as_double(0x7ff8000000000000LL) : s * g.scale * unscale;
+    double s = __longlong_as_double(0x7ff8000000000000LL);  // NaN unless the contraction succeeded
+    if (!bad) {
+      s = 0.0;
+      for (int sp = 0; sp < q.nsplit; ++sp)
+        s += (double)g.partials[(q.item0 + (int64_t)sp * npairs + p) * (GM * GM) + off];
+      s *= g.scale / ((double)row_scale(g.rows[q.row0 + i], g.op) * (double)row_scale(g.rows[q.row0 + j], g.op));
+    }
     g.out[q.out_off + (int64_t)i * q.n + j] = s;
     g.out[q.out_off + (int64_t)j * q.n + i] = s;
   }
@@ -459,11 +465,9 @@ __global__ void row_amax_kernel(const float4* __restrict__ X, int64_t q4_per_row
 }
 
 // Descriptors of one query over contiguous rows J + i * Q.
-__global__ void group_single_setup_kernel(GRow* rows, GItem* items, GQuery* query, GHeader* hdr, int64_t* elem0,
-                                          const float2* J, const float* amax, int64_t Q, int n, int nt, int nsplit,
-                                          int cps, int nchunks) {
+__global__ void group_single_setup_kernel(GRow* rows, GQuery* query, GHeader* hdr, int64_t* elem0, const float2* J,
+                                          const float* amax, int64_t Q, int n, int nt, int nsplit) {
   const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  const int npairs = nt * (nt + 1) / 2;
   if (t < n) {
     GRow r;
     r.J = J + t * Q;
@@ -471,24 +475,13 @@ __global__ void group_single_setup_kernel(GRow* rows, GItem* items, GQuery* quer
     for (int c = 0; c < 3; ++c) { r.c_hi[c] = 0.f; r.c_lo[c] = 0.f; }
     rows[t] = r;
   }
-  if (t < (int64_t)npairs * nsplit) {
-    const int sp = (int)(t / npairs), p = (int)(t % npairs);
-    int a = 0, rem = p;
-    while (rem >= nt - a) { rem -= nt - a; ++a; }
-    const int b = a + rem;
-    GItem w;
-    w.row_a = a * GM; w.row_b = b * GM;
-    w.na = min(GM, n - a * GM); w.nb = min(GM, n - b * GM);
-    w.chunk0 = sp; w.nchunks = (nchunks - sp + nsplit - 1) / nsplit; w.cstride = nsplit;
-    w.query = 0;
-    items[t] = w;
-  }
   if (t == 0) {
     GQuery q;
     q.row0 = 0; q.n = n; q.nt = nt; q.nsplit = nsplit; q.item0 = 0; q.out_off = 0;
     *query = q;
     GHeader h;
-    h.n_items = npairs * nsplit; h.n_queries = 1; h.n_elems = (int64_t)n * n;
+    h.n_items = nt * (nt + 1) / 2 * nsplit; h.n_queries = 1; h.n_elems = (int64_t)n * n;
+    h.n_evals = 0; h.reserved_ = 0;
     *hdr = h;
     elem0[0] = 0;
   }
@@ -510,8 +503,8 @@ int sms() {
 }
 
 struct SinglePlan {
-  int nt, npairs, nsplit, cps, nchunks, items;
-  size_t off_hdr, off_q, off_e, off_amax, off_rows, off_items, off_part, total;
+  int nt, npairs, nsplit, nchunks, items;
+  size_t off_hdr, off_q, off_e, off_amax, off_rows, off_part, total;
 };
 
 // Items of one query: at least two per SM for balance, otherwise as long as
@@ -521,10 +514,8 @@ SinglePlan plan_single(int64_t Q, int n) {
   p.nt = (n + GM - 1) / GM;
   p.npairs = p.nt * (p.nt + 1) / 2;
   p.nchunks = (int)((Q + CK - 1) / CK);
-  int nsplit = std::max(1, (2 * sms() + p.npairs - 1) / p.npairs);
-  nsplit = std::min(nsplit, p.nchunks);
-  p.cps = (p.nchunks + nsplit - 1) / nsplit;
-  p.nsplit = (p.nchunks + p.cps - 1) / p.cps;
+  const int nsplit = std::max(1, (2 * sms() + p.npairs - 1) / p.npairs);
+  p.nsplit = std::min(nsplit, p.nchunks);
   p.items = p.npairs * p.nsplit;
   auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
   p.off_hdr = 256;                                   // [0, 256): error flag
@@ -532,8 +523,7 @@ SinglePlan plan_single(int64_t Q, int n) {
   p.off_e = p.off_q + 256;
   p.off_amax = p.off_e + 256;
   p.off_rows = al(p.off_amax + (size_t)n * sizeof(float));
-  p.off_items = al(p.off_rows + (size_t)n * sizeof(GRow));
-  p.off_part = al(p.off_items + (size_t)p.items * sizeof(GItem));
+  p.off_part = al(p.off_rows + (size_t)n * sizeof(GRow));
   p.total = p.off_part + (size_t)p.items * GM * GM * sizeof(float);
   return p;
 }
@@ -641,8 +631,8 @@ int launch_group_single(const float2* Jw, int64_t Q, int n, int op, double* V, v
   g.queries = reinterpret_cast<const GQuery*>(base + p.off_q);
   g.elem0 = reinterpret_cast<const int64_t*>(base + p.off_e);
   g.rows = reinterpret_cast<const GRow*>(base + p.off_rows);
-  g.items = reinterpret_cast<const GItem*>(base + p.off_items);
   g.partials = reinterpret_cast<float*>(base + p.off_part);
+  g.max_items = p.items;
   g.err = reinterpret_cast<int*>(base);
   g.out = V;
   g.ncols = Q;
@@ -662,10 +652,9 @@ int launch_group_single(const float2* Jw, int64_t Q, int n, int op, double* V, v
     }
   }
   PI_CUDA(cudaMemsetAsync(g.err, 0, sizeof(int), s));
-  const int64_t nset = std::max<int64_t>(n, p.items);
-  group_single_setup_kernel<<<(unsigned)((nset + 255) / 256), 256, 0, s>>>(
-      const_cast<GRow*>(g.rows), const_cast<GItem*>(g.items), const_cast<GQuery*>(g.queries),
-      const_cast<GHeader*>(g.hdr), const_cast<int64_t*>(g.elem0), Jw, amax, Q, n, p.nt, p.nsplit, p.cps, p.nchunks);
+  group_single_setup_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(
+      const_cast<GRow*>(g.rows), const_cast<GQuery*>(g.queries), const_cast<GHeader*>(g.hdr),
+      const_cast<int64_t*>(g.elem0), Jw, amax, Q, n, p.nt, p.nsplit);
   PI_LAUNCHED("group_single_setup_kernel");
   CUtensorMap xmap;
   int rc = encode_row_map(&xmap, Jw, 2 * Q, n);

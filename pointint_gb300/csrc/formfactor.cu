@@ -187,10 +187,14 @@ struct Acc {
   }
 };
 
-template <int R>
+// SERVE: blockIdx.y indexes `evals` (serving evaluations: optional rotation of
+// the k directions, local-frame direction-major output, row maximum);
+// otherwise it indexes the batch's objects (largest first) and J is written
+// q-major with the origin phase.
+template <int R, bool SERVE>
 __global__ void __launch_bounds__(FF_THREADS, 3)
-ff_kernel(KGridDev kg, BatchDev b, float2* __restrict__ J, int scale_sqrt_w) {
-  const int oi = b.order[blockIdx.y];
+ff_kernel(KGridDev kg, BatchDev b, float2* __restrict__ J, int scale_sqrt_w, const EvalDev* __restrict__ evals) {
+  const int oi = SERVE ? evals[blockIdx.y].obj : b.order[blockIdx.y];
   const ObjDev od = b.objs[oi];
   const int nrb = (kg.L + R - 1) / R;
   const int ndt = (kg.M + 31) / 32;
@@ -206,6 +210,17 @@ ff_kernel(KGridDev kg, BatchDev b, float2* __restrict__ J, int scale_sqrt_w) {
     float4 h = kg.dir_hi[j], l = kg.dir_lo[j];
     dh = make_float3(h.x, h.y, h.z); dl = make_float3(l.x, l.y, l.z);
     inv_norm = h.w; dnorm = l.w;
+    if (SERVE && evals[blockIdx.y].rotate) {
+      // rotated object: its form factor at k is the unrotated one's at R^T k
+      // (|R^T k| = |k|); the direction is turned in FP64 and re-split.
+      const double* Rm = evals[blockIdx.y].R;
+      const double d0 = (double)h.x + (double)l.x, d1 = (double)h.y + (double)l.y, d2 = (double)h.z + (double)l.z;
+      double e[3];
+#pragma unroll
+      for (int a = 0; a < 3; ++a) e[a] = Rm[a] * d0 + Rm[3 + a] * d1 + Rm[6 + a] * d2;
+      dh = make_float3((float)e[0], (float)e[1], (float)e[2]);
+      dl = make_float3((float)(e[0] - (double)dh.x), (float)(e[1] - (double)dh.y), (float)(e[2] - (double)dh.z));
+    }
   }
   // radii r = rb + nrb * i: every warp sees small and large k alike, so the
   // warps of a CTA finish an element tile together.
@@ -326,6 +341,25 @@ ff_kernel(KGridDev kg, BatchDev b, float2* __restrict__ J, int scale_sqrt_w) {
 
   if (!active) return;
   acc.flush();
+  if (SERVE) {
+    const EvalDev& ev = evals[blockIdx.y];
+    float m = 0.f;
+#pragma unroll
+    for (int i = 0; i < R; ++i) {
+      const int r = rb + nrb * i;
+      if (r < kg.L) {
+        const int64_t q = (int64_t)r * kg.M + j;
+        cf v{acc.sre[i], acc.sim[i]};
+        if (km[i].hi * dnorm < 1e-10f) v = cf{0.f, 0.f};  // A(0) = 0 (affine_dof.cpp:64-65)
+        const float sw = kg.sqrtw[q];
+        v.re *= sw; v.im *= sw;
+        ev.dst[(int64_t)j * kg.L + r] = make_float2(v.re, v.im);
+        m = fmaxf(m, fmaxf(fabsf(v.re), fabsf(v.im)));
+      }
+    }
+    atomicMax(reinterpret_cast<unsigned*>(ev.amax), __float_as_uint(m));
+    return;
+  }
   // origin phase e^{i k.o}: dir . o formed in FP64 once per thread, then double-float.
   const double dox = (double)dh.x + (double)dl.x, doy = (double)dh.y + (double)dl.y,
                doz = (double)dh.z + (double)dl.z;
@@ -352,6 +386,8 @@ __global__ void to_double2_kernel(const float2* __restrict__ J, int64_t n, doubl
 }
 
 }  // namespace
+
+static int radii_per_thread(int L) { return L >= 32 ? 8 : L >= 4 ? 4 : 1; }
 
 int launch_prepare(pi_batch_impl* b, int only_index, cudaStream_t s) {
   std::vector<PrepObj> h(b->n_obj);
@@ -389,18 +425,65 @@ int launch_form_factors(const pi_kgrid_impl* kg, const pi_batch_impl* b, int sca
   if (b->n_obj == 0) return PI_OK;
   const KGridDev K = kg->dev;
   const BatchDev B = b->dev();
-  int R = K.L >= 32 ? 8 : K.L >= 4 ? 4 : 1;
+  int R = radii_per_thread(K.L);
   const int nrb = (K.L + R - 1) / R;
   const int ndt = (K.M + 31) / 32;
   const int64_t items = (int64_t)nrb * ndt;
   dim3 grid((unsigned)((items + FF_WARPS - 1) / FF_WARPS), (unsigned)b->n_obj);
   if (grid.y > 65535) return fail(PI_ERR_UNSUPPORTED, "more than 65535 objects in one batch");
   switch (R) {
-    case 8: ff_kernel<8><<<grid, FF_THREADS, 0, s>>>(K, B, J, scale_sqrt_w); break;
-    case 4: ff_kernel<4><<<grid, FF_THREADS, 0, s>>>(K, B, J, scale_sqrt_w); break;
-    default: ff_kernel<1><<<grid, FF_THREADS, 0, s>>>(K, B, J, scale_sqrt_w); break;
+    case 8: ff_kernel<8, false><<<grid, FF_THREADS, 0, s>>>(K, B, J, scale_sqrt_w, nullptr); break;
+    case 4: ff_kernel<4, false><<<grid, FF_THREADS, 0, s>>>(K, B, J, scale_sqrt_w, nullptr); break;
+    default: ff_kernel<1, false><<<grid, FF_THREADS, 0, s>>>(K, B, J, scale_sqrt_w, nullptr); break;
   }
   PI_LAUNCHED("ff_kernel");
+  return PI_OK;
+}
+
+int ff_serve_threads() { return FF_THREADS; }
+
+int ff_serve_grid_x(const pi_kgrid_impl* kg) {
+  const int R = radii_per_thread(kg->dev.L);
+  const int64_t items = (int64_t)((kg->dev.L + R - 1) / R) * ((kg->dev.M + 31) / 32);
+  return (int)((items + FF_WARPS - 1) / FF_WARPS);
+}
+
+const void* ff_serve_fn(const pi_kgrid_impl* kg) {
+  switch (radii_per_thread(kg->dev.L)) {
+    case 8: return reinterpret_cast<const void*>(ff_kernel<8, true>);
+    case 4: return reinterpret_cast<const void*>(ff_kernel<4, true>);
+    default: return reinterpret_cast<const void*>(ff_kernel<1, true>);
+  }
+}
+
+int launch_form_factors_serve(const pi_kgrid_impl* kg, const pi_batch_impl* lib, const EvalDev* evals, int n_evals,
+                              cudaStream_t s) {
+  if (n_evals <= 0) return PI_OK;
+  if (n_evals > 65535) return fail(PI_ERR_UNSUPPORTED, "more than 65535 evaluations in one launch");
+  KGridDev K = kg->dev;
+  BatchDev B = lib->dev();
+  float2* none = nullptr;
+  int scale = 1;
+  void* args[5] = {&K, &B, &none, &scale, const_cast<EvalDev**>(&evals)};
+  PI_CUDA(cudaLaunchKernel(ff_serve_fn(kg), dim3((unsigned)ff_serve_grid_x(kg), (unsigned)n_evals), dim3(FF_THREADS),
+                           args, 0, s));
+  count_launch();
+  return PI_OK;
+}
+
+namespace {
+__global__ void amax_commit_kernel(const EvalDev* __restrict__ evals, const int32_t* __restrict__ n_evals) {
+  const int n = *n_evals;
+  for (int e = threadIdx.x; e < n; e += blockDim.x) *evals[e].amax_keep = *evals[e].amax;
+}
+}  // namespace
+
+const void* amax_commit_fn() { return reinterpret_cast<const void*>(amax_commit_kernel); }
+int amax_commit_threads() { return 256; }
+
+int launch_amax_commit(const EvalDev* evals, const int32_t* n_evals, cudaStream_t s) {
+  amax_commit_kernel<<<1, 256, 0, s>>>(evals, n_evals);
+  PI_LAUNCHED("amax_commit_kernel");
   return PI_OK;
 }
 

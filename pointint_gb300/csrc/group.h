@@ -36,7 +36,7 @@ struct GRow {                          // 40 bytes
   float c_hi[3], c_lo[3];              // translation c = c_hi + c_lo
 };
 
-struct GItem {                         // 32 bytes
+struct GItem {                         // one work item, derived on the device from the query table
   int32_t row_a, row_b;                // first row of each tile (absolute row index)
   int32_t na, nb;                      // valid rows in each tile (1..128)
   int32_t chunk0, nchunks;             // k chunks chunk0 + c * cstride, c < nchunks
@@ -52,15 +52,15 @@ struct GQuery {                        // 32 bytes
   int64_t out_off;                     // V (n x n, FP64) at out + out_off
 };
 
-struct GHeader {                       // 16 bytes
+struct GHeader {                       // 24 bytes
   int32_t n_items, n_queries;
   int64_t n_elems;                     // sum of n^2 over queries
+  int32_t n_evals, reserved_;          // form-factor evaluations of the batch (serving)
 };
 
 struct GroupDev {                      // kernel argument; pointers fixed for the life of a graph
   const GHeader* hdr;
   const GRow* rows;
-  const GItem* items;
   const GQuery* queries;
   const int64_t* elem0;                // per query: prefix sum of n^2
   int64_t ncols;                       // complex columns per row
@@ -71,6 +71,7 @@ struct GroupDev {                      // kernel argument; pointers fixed for th
   const float4* dir_lo;
   const float2* kturn;                 // kmag / 2 pi (double-float), L entries
   float* partials;                     // n_items x 128 x 128
+  int64_t max_items;                   // capacity of `partials`; a launch with more items records an error
   int* err;                            // 0 = ok
   double* out;                         // output arena
   double scale;                        // 1 / (8 pi^3)
@@ -92,6 +93,35 @@ const void* group_contract_fn(int op, int phase, int tma);
 const void* group_reduce_fn();
 int group_reduce_threads();
 int group_prepare_attributes();
+
+#ifdef __CUDACC__
+// Work item `it` (split-major within its query: it - item0 = split * npairs + pair).
+__device__ __forceinline__ GItem group_item(const GroupDev& g, int it) {
+  int lo = 0, hi = g.hdr->n_queries - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (g.queries[mid].item0 <= it) lo = mid; else hi = mid - 1;
+  }
+  const GQuery q = g.queries[lo];
+  const int npairs = q.nt * (q.nt + 1) / 2;
+  const int local = (int)(it - q.item0);
+  const int sp = local / npairs;
+  int a = 0, rem = local - sp * npairs;
+  while (rem >= q.nt - a) { rem -= q.nt - a; ++a; }
+  const int b = a + rem;
+  const int nch = (int)((g.ncols + GROUP_CHUNK - 1) / GROUP_CHUNK);
+  GItem w;
+  w.row_a = q.row0 + a * GROUP_TILE;
+  w.row_b = q.row0 + b * GROUP_TILE;
+  w.na = min(GROUP_TILE, q.n - a * GROUP_TILE);
+  w.nb = min(GROUP_TILE, q.n - b * GROUP_TILE);
+  w.chunk0 = sp;
+  w.cstride = q.nsplit;
+  w.nchunks = (nch - sp + q.nsplit - 1) / q.nsplit;
+  w.query = lo;
+  return w;
+}
+#endif
 
 // 2D tensor map over n_rows contiguous rows of row_floats FP32 values, in the
 // contraction's 128-row x 32-value boxes, 128-byte swizzled.

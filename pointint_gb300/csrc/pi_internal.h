@@ -40,6 +40,7 @@ struct KGridDev {
   const float2* kmag;     // L: (hi, lo)
   const float* sqrtw;     // Q: sqrt(|w_q|)
   const float* sign;      // Q: sign(w_q), or nullptr when every weight is >= 0
+  const float2* kturn;    // L: kmag / 2 pi (hi, lo)
 };
 
 struct pi_kgrid_impl {
@@ -70,6 +71,20 @@ struct BatchDev {
   const int32_t* order;      // CTA y-index -> object (largest first)
   const float4* tri_pool;
   const float4* surf_pool;
+};
+
+// One form-factor evaluation of the serving path: library object `obj`,
+// optionally rotated (its form factors at k are the unrotated object's at
+// R^T k), written in the object-local frame (no origin phase), sqrt|w|-scaled
+// and direction-major (column j * L + r) to dst; the largest |Re|, |Im| goes
+// to *amax (FP32 bits, atomicMax) for the FP16 operand scale.
+struct EvalDev {          // 104 bytes
+  int32_t obj;
+  int32_t rotate;
+  float2* dst;
+  float* amax;            // zeroed before the launch; atomicMax target
+  float* amax_keep;       // the row's persistent maximum, copied from *amax after the evaluation
+  double R[9];            // row-major
 };
 
 struct HostObjInfo {
@@ -123,6 +138,17 @@ int launch_adjoint_elements(const pi_kgrid_impl* kg, const pi_batch_impl* b, con
 int launch_dof_gradients(const pi_kgrid_impl* kg, pi_batch_impl* b, const float2* Jw, const double* W_host,
                          double* grad, void* ws, size_t ws_bytes, cudaStream_t s);
 int launch_to_double2(const float2* J, int64_t n, double* out, cudaStream_t s);
+// Serving evaluations: grid (ff_serve_grid_x(kg), n_evals), ff_serve_threads().
+int ff_serve_grid_x(const pi_kgrid_impl* kg);
+int ff_serve_threads();
+const void* ff_serve_fn(const pi_kgrid_impl* kg);
+int launch_form_factors_serve(const pi_kgrid_impl* kg, const pi_batch_impl* lib, const EvalDev* evals, int n_evals,
+                              cudaStream_t s);
+// After the serving evaluations: *amax_keep = *amax for the first *n_evals evals
+// (one CTA of amax_commit_threads()).
+const void* amax_commit_fn();
+int amax_commit_threads();
+int launch_amax_commit(const EvalDev* evals, const int32_t* n_evals, cudaStream_t s);
 
 }  // namespace pi
 

@@ -129,3 +129,21 @@ def test_device_entry_points_fail_loudly_without_gpu():
         pc.compute_intersection_volume_cuda(g, g, kg)
     with pytest.raises(NotImplementedError):
         pc.compute_intersection_volume_cpu(g, g, kg)
+
+
+def test_server_fails_loudly_without_gpu():
+    """The serving entry points go through the C ABI and report the missing
+    device as a status (no host fallback)."""
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    from pointint_gb300 import geometry as G
+    from pointint_gb300.serving import Server
+    V, F = G.create_unit_cube_mesh()
+    with pytest.raises(_lib.PointIntError):
+        Server(K.standard_kgrid(3, 16), [G.SceneObject(G.make_triangle_mesh(V, F))], autotune=False)
+    srv = Server.__new__(Server)
+    srv._h = None
+    with pytest.raises(_lib.PointIntError) as ei:
+        _lib.check(_lib.lib().pi_server_submit(None, None, None, None))
+    assert ei.value.status == 1

@@ -1,0 +1,201 @@
+"""Serving path (pi_server_*): resident form factors, rigid-transform scene
+queries, continuous batching.
+
+Each scene's volume matrix is checked against the FP64 oracle evaluated on the
+transformed objects themselves (composed AffineDoF A' = R A, t' = R t + t_q,
+or moved vertices for TriangleMeshDoF), at the split-contraction contract
+1e-4 (conditioned relative error).  A query's result must not depend on the
+batch it ran in: the same scene alone and inside a burst of other scenes gives
+bit-identical matrices.
+"""
+import threading
+
+import numpy as np
+import pytest
+
+import pointint_gb300 as pg
+from pointint_gb300 import geometry as G
+from pointint_gb300.kgrid import standard_kgrid
+from pointint_gb300.serving import Server
+from test_gpu_parity import cond_rel_err
+
+pytestmark = pytest.mark.gpu
+
+SPLIT_TOL = 1e-4
+
+
+@pytest.fixture(scope="module")
+def kg():
+    return standard_kgrid(9, 16)  # 38 directions x 16 radii (L a multiple of 16)
+
+
+def library(rng):
+    out = []
+    V, F = G.create_unit_cube_mesh()
+    out.append(G.SceneObject(G.make_triangle_mesh(V, F)))
+    V, F = G.icosphere(2)
+    A = G.random_rotation(rng) @ np.diag([0.6, 1.3, 0.9]) @ G.random_rotation(rng).T
+    out.append(G.SceneObject(G.make_triangle_mesh(V, F), pg.DOF_AFFINE, G.affine_dofs(A, [0.3, -0.2, 0.1])))
+    V, F = G.icosphere(1)
+    V = V * (1 + 0.05 * rng.normal(size=(len(V), 1))) * 0.8
+    out.append(G.SceneObject(G.make_triangle_mesh(V, F), pg.DOF_TRIANGLE_MESH, V.reshape(-1).copy()))
+    P, N, R = G.create_sphere_pointcloud(200)
+    out.append(G.SceneObject(G.make_point_cloud(P * 0.7, N, R * 0.7), pg.DOF_AFFINE,
+                             G.affine_dofs(np.eye(3) + 0.1 * rng.normal(size=(3, 3)), [0.1, 0.0, -0.2])))
+    P, N, S, W = G.create_sphere_gaussians(200)
+    out.append(G.SceneObject(G.make_gaussian_splat(P * 0.6, N, S * 0.6, W * 0.36)))
+    V, F = G.box_mesh([0.8, 1.6, 0.5])
+    out.append(G.SceneObject(G.make_triangle_mesh(V, F), pg.DOF_AFFINE, G.affine_dofs(np.eye(3), [1.0, 0.5, 0.0])))
+    return out
+
+
+def transformed(obj, R, t):
+    """The library object under x' = R x + t, as an oracle object."""
+    if obj.dof_type == pg.DOF_TRIANGLE_MESH:
+        V = obj.dofs.reshape(-1, 3) @ R.T + t
+        return obj.geom, pg.DOF_TRIANGLE_MESH, V.reshape(-1)
+    d = obj.dofs
+    A0 = d[3:].reshape(3, 3)
+    t0 = d[:3]
+    return obj.geom, pg.DOF_AFFINE, G.affine_dofs(R @ A0, R @ t0 + t)
+
+
+def oracle_scene(orc, kg, lib, objects, rots, trans):
+    objs = []
+    for k, i in enumerate(objects):
+        geom, dt, dofs = transformed(lib[i], rots[k], trans[k])
+        objs.append(orc.Obj(geom.type, geom.elems, dt, dofs))
+    V, _, _ = orc.volume_matrix(objs, (kg.dirs, kg.kmag, kg.w))
+    return V
+
+
+def scene(rng, n_lib, n, p_rot):
+    objects = rng.integers(0, n_lib, size=n)
+    rots = np.array([G.random_rotation(rng) if rng.random() < p_rot else np.eye(3) for _ in range(n)])
+    trans = rng.normal(0.0, 0.5, size=(n, 3))
+    return objects, rots, trans
+
+
+@pytest.fixture(scope="module")
+def lib():
+    return library(np.random.default_rng(5))
+
+
+@pytest.mark.parametrize("p_rot", [0.0, 0.5])
+@pytest.mark.parametrize("precision", ["fp16x3", "bf16x3"])
+def test_scene_matches_oracle(cuda, orc, kg, lib, p_rot, precision):
+    rng = np.random.default_rng(11 + int(10 * p_rot))
+    objects, rots, trans = scene(rng, len(lib), 9, p_rot)
+    objects[-1] = objects[0]  # a repeated object
+    with Server(kg, lib, precision=precision, autotune=False) as srv:
+        V = srv.query(objects, rots, trans)
+    R = oracle_scene(orc, kg, lib, objects, rots, trans)
+    err = cond_rel_err(V, R).max()
+    print(f"\n[{precision}, p_rot={p_rot}] scene vs oracle: max cond rel err {err:.3e}")
+    assert np.array_equal(V, V.T)
+    assert err <= (SPLIT_TOL if precision == "fp16x3" else 1e-3)
+
+
+def test_same_result_alone_and_in_the_mix(cuda, kg, lib):
+    """The same scene alone, then inside a burst of 40 other scenes submitted
+    from 4 threads while batches run: bit-identical."""
+    rng = np.random.default_rng(3)
+    probe = scene(rng, len(lib), 7, 0.3)
+    others = [scene(rng, len(lib), int(rng.integers(2, 20)), 0.3) for _ in range(40)]
+    with Server(kg, lib, inflight_batches=2, max_batch_queries=8, autotune=False) as srv:
+        V_alone = srv.query(*probe)
+        tickets, lock = [], threading.Lock()
+
+        def feed(chunk):
+            for sc in chunk:
+                t = srv.submit(*sc)
+                with lock:
+                    tickets.append(t)
+
+        threads = [threading.Thread(target=feed, args=(others[k::4],)) for k in range(4)]
+        for th in threads:
+            th.start()
+        t_probe = srv.submit(*probe)
+        for th in threads:
+            th.join()
+        V_mix = srv.wait(t_probe)
+        for t in tickets:
+            srv.wait(t)
+        st = srv.stats()
+    print(f"\nbatches {st['batches']} for {st['completed']} queries, evaluations {st['evaluations']}, "
+          f"resident hits {st['resident_hits']}")
+    assert st["completed"] == 42 and st["failed"] == 0
+    assert st["batches"] < st["completed"]  # queries shared batches
+    assert np.array_equal(V_alone, V_mix)
+
+
+def test_burst_results_match_one_at_a_time(cuda, orc, kg, lib):
+    rng = np.random.default_rng(8)
+    scenes = [scene(rng, len(lib), int(rng.integers(2, 12)), 0.2) for _ in range(12)]
+    with Server(kg, lib, autotune=False) as srv:
+        tickets = [srv.submit(*sc) for sc in scenes]
+        Vs = [srv.wait(t) for t in tickets]
+    for sc, V in zip(scenes[:4], Vs[:4]):
+        R = oracle_scene(orc, kg, lib, *sc)
+        assert cond_rel_err(V, R).max() <= SPLIT_TOL
+
+
+def test_graphs_and_stream_launches_agree(cuda, kg, lib):
+    rng = np.random.default_rng(21)
+    scenes = [scene(rng, len(lib), 6, 0.3) for _ in range(5)]
+    out = []
+    for graphs in (True, False):
+        with Server(kg, lib, use_graphs=graphs, autotune=False) as srv:
+            out.append([srv.query(*sc) for sc in scenes])
+            if graphs:
+                assert srv.stats()["graph_launches"] == len(scenes)
+    for a, b in zip(*out):
+        assert np.array_equal(a, b)
+
+
+def test_small_budget_evicts_and_stays_correct(cuda, orc, kg, lib):
+    """A pool of a handful of rows: canonical rows are evicted (LRU) and
+    re-evaluated, and results do not change."""
+    row_bytes = ((kg.num_nodes + 31) // 32) * 32 * 8
+    rng = np.random.default_rng(4)
+    scenes = [scene(rng, len(lib), 4, 0.0) for _ in range(6)]
+    with Server(kg, lib, autotune=False) as srv:
+        ref = [srv.query(*sc) for sc in scenes]
+    small = dict(autotune=False, inflight_batches=1, max_batch_queries=1, max_batch_rows=8, max_batch_evals=8)
+    budget0 = 256 * 1024 * 1024
+    with Server(kg, lib, hbm_budget_bytes=budget0, **small) as srv:
+        pool0 = srv.stats()["pool_rows"]
+    budget = budget0 - (pool0 - 5) * row_bytes  # the same arenas, five pool rows
+    with Server(kg, lib, hbm_budget_bytes=budget, **small) as srv:
+        pool = srv.stats()["pool_rows"]
+        got = [srv.query(*sc) for sc in scenes]
+        st = srv.stats()
+    print(f"\npool rows {pool}, evictions {st['evictions']}")
+    for a, b in zip(ref, got):
+        np.testing.assert_allclose(a, b, rtol=0, atol=1e-12 * np.abs(a).max())
+    if pool < len(lib):
+        assert st["evictions"] > 0
+
+
+def test_cancel_and_invalid_queries(cuda, kg, lib):
+    rng = np.random.default_rng(2)
+    with Server(kg, lib, inflight_batches=1, max_batch_queries=1, autotune=False) as srv:
+        ts = [srv.submit(*scene(rng, len(lib), 10, 0.5)) for _ in range(8)]
+        last = ts[-1]
+        try:
+            srv.cancel(last)
+            cancelled = True
+        except pg.PointIntError:
+            cancelled = False  # already admitted
+        for t in ts[:-1]:
+            srv.wait(t)
+        if cancelled:
+            assert srv.poll(last) == "cancelled"
+        else:
+            srv.wait(last)
+        with pytest.raises(pg.PointIntError):
+            srv.submit([0, len(lib)])  # index out of range
+        bad = np.eye(3)[None].repeat(2, 0)
+        bad[1] = np.diag([1.0, 1.0, -1.0])  # a reflection is not a rigid motion
+        with pytest.raises(pg.PointIntError):
+            srv.submit([0, 1], rotations=bad)
