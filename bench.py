@@ -49,6 +49,10 @@ def parse():
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--cpu-seconds", type=float, default=12.0)
+    p.add_argument("--no-serve", action="store_true", help="skip the serving measurements")
+    p.add_argument("--serve-queries", type=int, default=160,
+                   help="scene-stream sample size (the stream workload has 10,000 queries)")
+    p.add_argument("--serve-burst", type=int, default=200, help="256-object scene queries in the warm burst")
     p.add_argument("--objects", type=int, default=256,
                    help="object count of the matrix workload (256 = the benchmark; smaller only for profiling)")
     return p.parse_args()
@@ -304,6 +308,8 @@ def run_gb300(args):
 
     if rank == 0 and not args.no_e2e:
         line["e2e"] = e2e_host(kg, objs, precision, args.steps, evals_step, world)
+    if rank == 0 and not args.no_serve and args.objects == 256:
+        line["serving"] = serving_bench(args, kg, objs, batch, contraction, flush)
     if rank == 0 and world == 1 and not args.no_cpu:
         try:
             line["cpu_baseline"] = {k: v for k, v in cpu_baseline_matrix256(objs, kg, args.cpu_seconds).items()
@@ -318,6 +324,145 @@ def run_gb300(args):
 
 
 FF_TRAFFIC_BYTES_PER_LAUNCH = None
+
+
+def _pcts(ms):
+    a = np.sort(np.asarray(ms))
+    return {"p50_ms": float(np.percentile(a, 50)), "p99_ms": float(np.percentile(a, 99)), "n": int(len(a))}
+
+
+def serving_bench(args, kg, objs, batch, contraction, flush):
+    """Resident-J serving: (a) the 256-object matrix re-queried under jittered
+    translations (warm: form factors resident, translations as phases in the
+    FP16-split contraction) against the plain FP32 GPU form; (b) a sample of
+    the scene stream (N ~ logU[2,512], 20% rotated objects) at saturation and
+    under Poisson arrivals at half that rate, against one-query-at-a-time plain
+    FP32 (every form factor re-evaluated, FP32 contraction)."""
+    import threading
+    import torch
+    from pointint_gb300 import configs, core, geometry as G
+    from pointint_gb300.serving import Server
+    out = {}
+    n = len(objs)
+    rng = np.random.default_rng(7)
+    ids = np.arange(n, dtype=np.int32)
+
+    # plain FP32 GPU form of one matrix: DoF transform + form factors + FP32 contraction
+    Jw = torch.empty((n, kg.num_nodes), dtype=torch.complex64, device="cuda")
+    V = torch.empty((n, n), dtype=torch.float64, device="cuda")
+    ws = core.Workspace()
+    stream = torch.cuda.current_stream()
+    plain = []
+    for i in range(4):
+        flush.zero_()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        batch.prepare()
+        core.form_factors(kg, batch, True, out=Jw)
+        core.contract(kg, Jw, "fp32", out=V, workspace=ws)
+        b.record(stream)
+        b.synchronize()
+        if i:
+            plain.append(a.elapsed_time(b))
+    plain_ms = statistics.median(plain)
+    fp32_contract_ms = contraction.get("fp32", {}).get("ms")
+
+    with Server(kg, objs, precision="fp16x3") as srv:
+        t0 = time.perf_counter()
+        srv.query(ids, None, np.zeros((n, 3)))          # cold: every row evaluated
+        cold_s = time.perf_counter() - t0
+        seq = []
+        for _ in range(30):                                # unloaded latency
+            t = srv.submit(ids, None, rng.normal(0.0, 0.5, size=(n, 3)))
+            srv.wait(t)
+            a, _, c = srv.times(t)
+            seq.append((c - a) / 1e6)
+            srv.release(t)
+        trs = [rng.normal(0.0, 0.5, size=(n, 3)) for _ in range(args.serve_burst)]
+        t0 = time.perf_counter()
+        ts = [srv.submit(ids, None, tr) for tr in trs]
+        for t in ts:
+            srv.wait(t)
+        burst_s = time.perf_counter() - t0
+        lat = []
+        for t in ts:
+            a, _, c = srv.times(t)
+            lat.append((c - a) / 1e6)
+        st = srv.stats()
+        # accuracy of the last scene: FP64 contraction of the plain path's J for the same objects
+        tr = trs[-1]
+        moved = [G.SceneObject(o.geom, o.dof_type, np.concatenate([o.dofs[:3] + tr[k], o.dofs[3:]]))
+                 for k, o in enumerate(objs)]
+        Jm = core.form_factors(kg, core.ObjectBatch(moved), True)
+        X = torch.view_as_real(Jm).reshape(n, -1).double()
+        R = ((X @ X.T) / (8 * np.pi ** 3)).cpu().numpy()
+        del X, Jm
+        d = np.sqrt(np.abs(np.outer(np.diag(R), np.diag(R))))
+        err = float((np.abs(ts[-1].V - R) / np.maximum(np.abs(R), 1e-3 * d)).max())
+    vps = args.serve_burst / burst_s
+    out["matrix256_scenes"] = {
+        "what": "256-object scene re-queried with per-object translations N(0,0.5^2): resident J, phases fused "
+                "into the FP16-split tensor-core contraction, continuous batching, CUDA graphs",
+        "vol_matrix_per_s": vps, "burst_queries": args.serve_burst, "burst_latency": _pcts(lat),
+        "unloaded_latency": _pcts(seq), "cold_first_query_ms": cold_s * 1e3,
+        "max_rel_err_vs_fp64_contraction": err, "precision": "fp16x3",
+        "plain_fp32_vol_matrix_per_s": 1e3 / plain_ms, "plain_fp32_ms": plain_ms,
+        "speedup_vs_plain_fp32": vps * plain_ms / 1e3,
+        "fp32_contraction_only_vol_matrix_per_s": (1e3 / fp32_contract_ms) if fp32_contract_ms else None,
+        "speedup_vs_fp32_contraction_only": (vps * fp32_contract_ms / 1e3) if fp32_contract_ms else None,
+        "batches": st["batches"], "graph_launches": st["graph_launches"],
+        "tuned_items_per_sm": st["tuned_items_per_sm"]}
+
+    # scene stream sample
+    _, lib, queries, _, meta = configs.serving_stream(seed=2, n_queries=args.serve_queries, kgrid=False)
+    with Server(kg, lib, precision="fp16x3") as srv:
+        srv.query(np.arange(len(lib), dtype=np.int32), None, None)  # library rows resident
+        t0 = time.perf_counter()
+        ts = [srv.submit(*q) for q in queries]
+        for t in ts:
+            srv.wait(t)
+        sat_s = time.perf_counter() - t0
+        sat_lat = [(srv.times(t)[2] - srv.times(t)[0]) / 1e6 for t in ts]
+        qps = len(queries) / sat_s
+        # open-loop Poisson arrivals at half the saturated rate
+        half = queries[: max(1, len(queries) // 2)]
+        gaps = np.random.default_rng(3).exponential(2.0 / qps, size=len(half))
+        tickets = []
+
+        def feed():
+            t_start = time.perf_counter()
+            due = np.cumsum(gaps)
+            for k, q in enumerate(half):
+                dt = due[k] - (time.perf_counter() - t_start)
+                if dt > 0:
+                    time.sleep(dt)
+                tickets.append(srv.submit(*q))
+
+        th = threading.Thread(target=feed)
+        th.start()
+        th.join()
+        for t in tickets:
+            srv.wait(t)
+        poi_lat = [(srv.times(t)[2] - srv.times(t)[0]) / 1e6 for t in tickets]
+        st = srv.stats()
+    # one query at a time, plain FP32: every form factor evaluated, FP32 contraction
+    base = []
+    for objects, rot, trans in queries[:8]:
+        sc = [G.SceneObject(lib[o].geom, lib[o].dof_type, G.affine_dofs(rot[k], trans[k]))
+              for k, o in enumerate(objects)]
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        core.volume_matrix(kg, sc, "fp32")
+        torch.cuda.synchronize()
+        base.append(time.perf_counter() - t0)
+    out["scene_stream"] = {
+        "workload": meta["workload"], "sample_queries": len(queries), "mean_objects": meta["mean_objects"],
+        "saturated_queries_per_s": qps, "saturated_latency": _pcts(sat_lat),
+        "poisson_rate_hz": qps / 2, "poisson_latency": _pcts(poi_lat),
+        "plain_fp32_one_at_a_time_queries_per_s": len(base) / sum(base), "plain_fp32_sample": len(base),
+        "speedup_vs_plain_fp32_one_at_a_time": qps * sum(base) / len(base),
+        "evaluations": st["evaluations"], "batches": st["batches"], "precision": "fp16x3"}
+    return out
 
 
 def e2e_host(kg, objs, precision, steps, evals_step, world):

@@ -14,6 +14,10 @@ definitions exactly; seeds and mix ratios are recorded in ``meta``.
                   Lebedev-5810 (N_k = 743,680)
   surfels64       64 objects x 50,000 disks (and the same as Gaussians),
                   area-uniform samples of matrix256 shapes, L=64 x Lebedev-1202
+  serving_stream  library of spheres / ellipsoids meshed with 1k-50k tris
+                  (log-uniform); scenes of N ~ logU[2, 512] library objects,
+                  each translated by N(0, 0.5^2) and rotated with probability
+                  0.2; Poisson arrival times; L=64 x Lebedev-1202
 """
 from __future__ import annotations
 
@@ -108,3 +112,45 @@ def large_mesh(seed: int = 0, n_objects: int = 32, frequency: int = 100, kgrid=T
     meta = {"workload": f"{n_objects} star-shaped solids x {len(F)} tris (SH degree<=8, N(0,0.05^2))",
             "seed": seed, "n_triangles_each": int(len(F)), "n_k": 743680}
     return kg, objs, meta
+
+
+def serving_stream(seed: int = 0, n_library: int = 64, n_queries: int = 10000, p_rot: float = 0.2,
+                   n_min: int = 2, n_max: int = 512, rate_hz: float = 100.0, kgrid=True):
+    """Scene-query stream: (kgrid, library, queries, arrival_s, meta).
+
+    Library meshes are geodesic spheres of frequency f (20 f^2 triangles, f in
+    7..50 for 1k-50k triangles, log-uniform), half of them stretched into
+    ellipsoids by R diag(U[0.5,1.5]^3) R'.  A query is (objects, rotations,
+    translations) with N log-uniform in [n_min, n_max] objects drawn with
+    replacement.  Arrivals are a Poisson process of rate rate_hz."""
+    rng = np.random.default_rng(seed)
+    cache = {}
+    lib, tris = [], []
+    for i in range(n_library):
+        t = float(np.exp(rng.uniform(np.log(1000.0), np.log(50000.0))))
+        f = int(min(50, max(7, round(np.sqrt(t / 20.0)))))
+        if f not in cache:
+            cache[f] = G.geodesic_sphere(f)
+        V, F = cache[f]
+        if i % 2:
+            R = G.random_rotation(rng)
+            V = V @ (R @ np.diag(rng.uniform(0.5, 1.5, size=3)) @ R.T).T
+        lib.append(G.SceneObject(G.make_triangle_mesh(V, F)))
+        tris.append(len(F))
+    queries = []
+    for _ in range(n_queries):
+        n = int(min(n_max, max(n_min, round(np.exp(rng.uniform(np.log(n_min), np.log(n_max)))))))
+        objects = rng.integers(0, n_library, size=n).astype(np.int32)
+        rot = np.zeros((n, 3, 3))
+        for k in range(n):
+            rot[k] = G.random_rotation(rng) if rng.random() < p_rot else np.eye(3)
+        trans = rng.normal(0.0, 0.5, size=(n, 3))
+        queries.append((objects, rot, trans))
+    arrival = np.cumsum(rng.exponential(1.0 / rate_hz, size=n_queries))
+    kg = standard_kgrid(59, 64) if kgrid else None
+    meta = {"workload": f"scene stream: N ~ logU[{n_min},{n_max}] of {n_library} library meshes "
+                        f"(geodesic spheres/ellipsoids, {min(tris)}-{max(tris)} tris), translations N(0,0.5^2), "
+                        f"rotation p={p_rot}, Poisson arrivals",
+            "seed": seed, "n_library": n_library, "library_tris": tris, "n_queries": n_queries,
+            "mean_objects": float(np.mean([len(q[0]) for q in queries])), "p_rot": p_rot}
+    return kg, lib, queries, arrival, meta
