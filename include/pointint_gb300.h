@@ -266,7 +266,7 @@ typedef struct {
   int32_t precision;         /* PI_CONTRACT_FP16X3 (0 = default) or PI_CONTRACT_BF16X3 */
   int32_t use_graphs;        /* 1: each batch is one CUDA graph launch; 0: plain stream launches; -1 = 1 */
   int32_t autotune;          /* 1: time work-item sizes at creation; 0: built-in sizes; -1 = 1 */
-  int32_t reserved_;
+  int32_t items_per_sm_x4;   /* > 0: work items per SM for every scene size, in quarters (overrides autotune) */
 } pi_server_config;
 
 typedef struct {

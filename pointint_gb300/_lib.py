@@ -43,7 +43,7 @@ class ServerConfig(ctypes.Structure):
     _fields_ = [("hbm_budget_bytes", ctypes.c_int64), ("max_batch_queries", ctypes.c_int32),
                 ("max_batch_rows", ctypes.c_int32), ("max_batch_evals", ctypes.c_int32),
                 ("inflight_batches", ctypes.c_int32), ("precision", ctypes.c_int32),
-                ("use_graphs", ctypes.c_int32), ("autotune", ctypes.c_int32), ("reserved_", ctypes.c_int32)]
+                ("use_graphs", ctypes.c_int32), ("autotune", ctypes.c_int32), ("items_per_sm_x4", ctypes.c_int32)]
 
 
 class Query(ctypes.Structure):

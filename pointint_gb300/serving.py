@@ -43,7 +43,7 @@ class Server:
     def __init__(self, kg: KGrid, library: list[SceneObject], *, hbm_budget_bytes: int = 0,
                  max_batch_queries: int = 0, max_batch_rows: int = 0, max_batch_evals: int = 0,
                  inflight_batches: int = 0, precision: str = "fp16x3", use_graphs: bool = True,
-                 autotune: bool = True):
+                 autotune: bool = True, items_per_sm: float = 0.0):
         if precision not in PRECISIONS:
             raise ValueError(f"precision must be one of {sorted(PRECISIONS)}")
         self._kg = kg                                   # keeps the device k-grid alive
@@ -51,7 +51,8 @@ class Server:
         self._hold = library
         arr = (_lib.PiObject * len(self._objs))(*self._objs)
         cfg = ServerConfig(hbm_budget_bytes, max_batch_queries, max_batch_rows, max_batch_evals, inflight_batches,
-                           PRECISIONS[precision], 1 if use_graphs else 0, 1 if autotune else 0, 0)
+                           PRECISIONS[precision], 1 if use_graphs else 0, 1 if autotune else 0,
+                           int(round(4 * items_per_sm)))
         h = ctypes.c_void_p()
         check(_lib.lib().pi_server_create(kg.handle(), arr, len(self._objs), ctypes.byref(cfg), ctypes.byref(h)))
         self._h = h
