@@ -507,14 +507,15 @@ struct SinglePlan {
   size_t off_hdr, off_q, off_e, off_amax, off_rows, off_part, total;
 };
 
-// Items of one query: at least two per SM for balance, otherwise as long as
-// possible (one partial tile per item).
+// Items of one query: up to two per SM (rounded down, so that no CTA gets a
+// third item and sets the kernel's length), otherwise as long as possible
+// (one partial tile per item).
 SinglePlan plan_single(int64_t Q, int n) {
   SinglePlan p;
   p.nt = (n + GM - 1) / GM;
   p.npairs = p.nt * (p.nt + 1) / 2;
   p.nchunks = (int)((Q + CK - 1) / CK);
-  const int nsplit = std::max(1, (2 * sms() + p.npairs - 1) / p.npairs);
+  const int nsplit = std::max(1, (2 * sms()) / p.npairs);
   p.nsplit = std::min(nsplit, p.nchunks);
   p.items = p.npairs * p.nsplit;
   auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };

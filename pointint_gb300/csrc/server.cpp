@@ -320,9 +320,11 @@ int nsplit_for(const Server& S, int n, int tuned_q4) {
   const int nt = (n + GROUP_TILE - 1) / GROUP_TILE;
   const int npairs = nt * (nt + 1) / 2;
   const int target = std::max(1, tuned_q4 * S.sms / 4);
-  int ns = std::max(1, (target + npairs - 1) / npairs);
   const int rb = std::max(1, S.kg->L / GROUP_CHUNK);
-  ns = (ns + rb - 1) / rb * rb;
+  // rounded down (to a multiple of rb, at least rb) so a query alone does not
+  // leave a few CTAs with one item more than the rest
+  int ns = std::max(1, target / npairs) / rb * rb;
+  ns = std::max(ns, rb);
   return (int)std::min<int64_t>(ns, S.nch);
 }
 
