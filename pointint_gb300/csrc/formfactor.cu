@@ -192,7 +192,7 @@ struct Acc {
 // otherwise it indexes the batch's objects (largest first) and J is written
 // q-major with the origin phase.
 template <int R, bool SERVE>
-__global__ void __launch_bounds__(FF_THREADS, 3)
+__global__ void __launch_bounds__(FF_THREADS, 4)
 ff_kernel(KGridDev kg, BatchDev b, float2* __restrict__ J, int scale_sqrt_w, const EvalDev* __restrict__ evals) {
   const int oi = SERVE ? evals[blockIdx.y].obj : b.order[blockIdx.y];
   const ObjDev od = b.objs[oi];
@@ -257,35 +257,25 @@ ff_kernel(KGridDev kg, BatchDev b, float2* __restrict__ J, int scale_sqrt_w, con
           const float s2 = fmaf(dh.x, e2.x, fmaf(dh.y, e2.y, dh.z * e2.z));
           const float sp = fmaxf(fmaxf(fabsf(s1), fabsf(s2)), fabsf(s2 - s1));
           const TriPoly tp = tri_series_coeffs(s1, s2, g);
-          uint32_t gmask = 0;
-          // Branch-free pass: the centroid Taylor series at every radius (the
-          // radii where the spread kmag*sp >= 2 are masked and redone below).
+          // vertex phases relative to the centroid (a = m - (e1 + e2)/3, b = a + e1, c = a + e2)
+          const float da = -(s1 + s2) * (1.0f / 3.0f), db = da + s1, dc = da + s2;
 #pragma unroll
           for (int i = 0; i < R; ++i) {
-            const bool tay = km[i].hi * sp < 2.0f;
-            gmask |= (tay ? 0u : 1u) << i;
-            const cf S = tri_series_eval(tp, km[i].hi);
-            const cf P = cis(df_mul_un(km[i], sm));
-            const float re = fmaf(P.re, S.re, fmaf(-P.im, S.im, acc.re[i]));
-            const float im = fmaf(P.re, S.im, fmaf(P.im, S.re, acc.im[i]));
-            acc.re[i] = tay ? re : acc.re[i];
-            acc.im[i] = tay ? im : acc.im[i];
-          }
-          if (gmask) {
-            // Large-spread radii: vertex phases in double-float
-            // (a = m - (e1 + e2)/3, b = a + e1, c = a + e2).
-            const df d1 = cdot(dh, dl, e1), d2 = cdot(dh, dl, e2);
-            const df sa = df_add(sm, df_div3(df_add(d1, d2)) * -1.0f);
-            const df sb = df_add(sa, d1), sc = df_add(sa, d2);
-#pragma unroll
-            for (int i = 0; i < R; ++i) {
-              if (gmask & (1u << i)) {
-                const cf v = tri_generic(cis(df_mul(km[i], sa)), cis(df_mul(km[i], sb)), cis(df_mul(km[i], sc)),
-                                         km[i].hi * d1.hi, km[i].hi * d2.hi);
-                acc.re[i] = fmaf(g, v.re, acc.re[i]);
-                acc.im[i] = fmaf(g, v.im, acc.im[i]);
-              }
+            const float k = km[i].hi;
+            const cf P = cis(df_mul_un(km[i], sm));  // centroid phase, double-float
+            cf T;
+            if (k * sp < 2.0f) {
+              T = tri_series_eval(tp, k);  // centroid Taylor series, gamma folded in
+            } else {
+              // Large spread: e[pa, pb, pc] = e^{i k.m} e[k da, k db, k dc].  The
+              // relative phases are FP32 products: their error |k d| 6e-8 rad
+              // multiplies a term of size ~1/|k d|^2 here.
+              const cf v = tri_generic(cis(df{k * da, 0.f}), cis(df{k * db, 0.f}), cis(df{k * dc, 0.f}), k * s1,
+                                       k * s2);
+              T = cf{g * v.re, g * v.im};
             }
+            acc.re[i] = fmaf(P.re, T.re, fmaf(-P.im, T.im, acc.re[i]));
+            acc.im[i] = fmaf(P.re, T.im, fmaf(P.im, T.re, acc.im[i]));
           }
           if (((base + e) & (FF_CHUNK - 1)) == FF_CHUNK - 1) acc.flush();
         }
