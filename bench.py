@@ -50,6 +50,7 @@ def parse():
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--cpu-seconds", type=float, default=12.0)
     p.add_argument("--no-serve", action="store_true", help="skip the serving measurements")
+    p.add_argument("--no-configs", action="store_true", help="skip the other workload configurations")
     p.add_argument("--serve-queries", type=int, default=160,
                    help="scene-stream sample size (the stream workload has 10,000 queries)")
     p.add_argument("--serve-burst", type=int, default=200, help="256-object scene queries in the warm burst")
@@ -310,6 +311,8 @@ def run_gb300(args):
         line["e2e"] = e2e_host(kg, objs, precision, args.steps, evals_step, world)
     if rank == 0 and not args.no_serve and args.objects == 256:
         line["serving"] = serving_bench(args, kg, objs, batch, contraction, flush)
+    if rank == 0 and not args.no_configs and args.objects == 256:
+        line["configs"] = configs_bench(args, flush)
     if rank == 0 and world == 1 and not args.no_cpu:
         try:
             line["cpu_baseline"] = {k: v for k, v in cpu_baseline_matrix256(objs, kg, args.cpu_seconds).items()
@@ -333,6 +336,92 @@ FF_TRAFFIC_BYTES_PER_LAUNCH = 4.73e6 * 656896 / 82112
 def _pcts(ms):
     a = np.sort(np.asarray(ms))
     return {"p50_ms": float(np.percentile(a, 50)), "p99_ms": float(np.percentile(a, 99)), "n": int(len(a))}
+
+
+def _timed(fn, flush, reps=3):
+    """Median CUDA-event time (ms) of fn() over reps runs after one warm-up, L2 flushed before each."""
+    import torch
+    fn()
+    torch.cuda.synchronize()
+    ts = []
+    for _ in range(reps):
+        flush.zero_()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        fn()
+        b.record()
+        b.synchronize()
+        ts.append(a.elapsed_time(b))
+    return statistics.median(ts)
+
+
+def configs_bench(args, flush):
+    """The other workload configurations, each timed on the GPU (samples where
+    the full configuration would take more than a few seconds):
+      pair_sweep   cube x icosphere-3 at 64 offsets, L=32 x Lebedev-302; volumes
+                   checked against the FP64 oracle on 8 of the 64 pairs
+      large_mesh   2 of the 32 star-shaped 200,000-triangle solids, L=128 x
+                   Lebedev-5810 (N_k = 743,680)
+      surfels64    8 of the 64 objects x 50,000 disks, forward volume matrix and
+                   the backward pass to per-disk positions and normals"""
+    import torch
+    from pointint_gb300 import configs, core
+    out = {}
+    # pair sweep
+    kg1, cube, spheres, offsets, meta1 = configs.pair_sweep()
+    b1 = core.ObjectBatch([cube] + spheres)
+    Jw = torch.empty((len(spheres) + 1, kg1.num_nodes), dtype=torch.complex64, device="cuda")
+    V1 = {}
+
+    def sweep():
+        core.form_factors(kg1, b1, True, out=Jw)
+        V1["V"] = core.contract(kg1, Jw, "fp32")
+    ms = _timed(sweep, flush)
+    vols = V1["V"][0, 1:].cpu().numpy()
+    evals1 = (cube.geom.num_elements() + spheres[0].geom.num_elements()) * kg1.num_nodes * len(spheres)
+    try:
+        from oracle import oracle as orc
+        orc.build()
+        ref = [orc.pair_volume(orc.Obj(cube.geom.type, cube.geom.elems, cube.dof_type, cube.dofs),
+                               orc.Obj(s.geom.type, s.geom.elems, s.dof_type, s.dofs),
+                               (kg1.dirs, kg1.kmag, kg1.w))["volume"] for s in spheres[:8]]
+        err = float(np.max(np.abs(vols[:8] - np.array(ref)) / np.maximum(np.abs(ref), 1e-12)))
+    except Exception as exc:  # the oracle must not break the GPU line
+        err = f"oracle unavailable: {exc}"
+    out["pair_sweep"] = {"workload": meta1["workload"], "ms": ms, "tri_k_evals_per_s": evals1 / (ms / 1e3),
+                         "pairs_per_s": len(spheres) / (ms / 1e3), "max_rel_err_vs_oracle_8_pairs": err}
+    del b1, Jw
+    # large mesh sample
+    kg3, objs3, meta3 = configs.large_mesh(n_objects=2)
+    b3 = core.ObjectBatch(objs3)
+    J3 = torch.empty((len(objs3), kg3.num_nodes), dtype=torch.complex64, device="cuda")
+    ms = _timed(lambda: core.form_factors(kg3, b3, True, out=J3), flush, reps=2)
+    evals3 = meta3["n_triangles_each"] * len(objs3) * kg3.num_nodes
+    out["large_mesh"] = {"workload": meta3["workload"], "sample_objects": len(objs3), "n_k": kg3.num_nodes,
+                         "ms": ms, "tri_k_evals_per_s": evals3 / (ms / 1e3),
+                         "full_config_seconds_at_this_rate": 32 * meta3["n_triangles_each"] * kg3.num_nodes / (evals3 / (ms / 1e3))}
+    del b3, J3
+    # surfels sample: forward and backward
+    kg4, objs4, meta4 = configs.surfels64(n_objects=8)
+    scene = core.Scene(kg4, objs4)
+    c0, n0 = scene.surfel_params()
+    res = {}
+
+    def fwd():
+        res["L"] = scene.volume_matrix_of_surfels(c0, n0).sum()
+
+    def fwd_bwd():
+        c = c0.clone().requires_grad_(True)
+        n = n0.clone().requires_grad_(True)
+        scene.volume_matrix_of_surfels(c, n).sum().backward()
+        res["g"] = c.grad
+    ms_f = _timed(fwd, flush, reps=2)
+    ms_fb = _timed(fwd_bwd, flush, reps=2)
+    evals4 = sum(o.geom.num_elements() for o in objs4) * kg4.num_nodes
+    out["surfels64"] = {"workload": meta4["workload"], "sample_objects": len(objs4), "forward_ms": ms_f,
+                        "forward_disk_k_evals_per_s": evals4 / (ms_f / 1e3), "forward_backward_ms": ms_fb,
+                        "backward_over_forward": (ms_fb - ms_f) / ms_f}
+    return out
 
 
 def serving_bench(args, kg, objs, batch, contraction, flush):
