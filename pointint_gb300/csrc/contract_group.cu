@@ -221,12 +221,14 @@ group_split3_kernel(const GroupDev g, const __grid_constant__ CUtensorMap xmap) 
         const bool diag = w.row_a == w.row_b;
         const int nrows = box == 0 ? w.na : (diag ? 0 : w.nb);
         const int rbase = box == 0 ? w.row_a : w.row_b;
+        // a tile whose rows are consecutive rows of the map loads by TMA
+        const int tma_row = (g.tile_tma && nrows > 0) ? g.rows[rbase].tma_row : -1;
         // lane l holds the row pointers of rows l, l+32, l+64, l+96
         unsigned long long myrow[4];
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
           const int r = lane + 32 * k;
-          myrow[k] = r < nrows ? reinterpret_cast<unsigned long long>(g.rows[rbase + r].J) : 0ull;
+          myrow[k] = (tma_row < 0 && r < nrows) ? reinterpret_cast<unsigned long long>(g.rows[rbase + r].J) : 0ull;
         }
         for (int c = 0; c < w.nchunks; ++c, ++gc) {
           const int s = (int)(gc % NST);
@@ -236,24 +238,36 @@ group_split3_kernel(const GroupDev g, const __grid_constant__ CUtensorMap xmap) 
           ok = __all_sync(0xffffffffu, ok);
           if (!ok) break;
           const int64_t col0 = ((int64_t)w.chunk0 + (int64_t)c * w.cstride) * CK;
-          const int npieces = (int)min((int64_t)CK, g.ncols - col0) / 2;  // 16-byte pieces (2 complex)
           const uint32_t st = smem_u32(smem + s * STAGE) + (uint32_t)(box * BOXB);
-          const int64_t coff = (col0 + 2 * piece) * (int64_t)sizeof(float2);
-          const bool active = piece < npieces;
-          // Half-warp h copies row 2m + h: 16 lanes x 16 B = the row's 256-byte
-          // chunk.  The row pointer comes from its owner lane by shuffle.
-#pragma unroll
-          for (int k = 0; k < 4; ++k) {
-            if (32 * k >= nrows) break;  // warp-uniform
-#pragma unroll 4
-            for (int m = 0; m < 16; ++m) {
-              const int r = 32 * k + 2 * m + rpar;
-              const unsigned long long base = __shfl_sync(0xffffffffu, myrow[k], (2 * m + rpar) & 31);
-              if (active && r < nrows)
-                cp_async16(st + stage_off(r, piece), reinterpret_cast<const void*>(base + coff));
+          const uint32_t bar = smem_u32(&load_bar[s]);
+          if (tma_row >= 0) {
+            // one arrival per lane as in the gather: lane 0's carries the bytes
+            if (lane == 0) {
+              mbar_expect_tx(bar, BOXB);
+              tma_load_2d(st, &xmap, (int)(col0 * 2), tma_row, bar);
+              tma_load_2d(st + HALF, &xmap, (int)(col0 * 2) + CK, tma_row, bar);
+            } else {
+              mbar_arrive(bar);
             }
+          } else {
+            const int npieces = (int)min((int64_t)CK, g.ncols - col0) / 2;  // 16-byte pieces (2 complex)
+            const int64_t coff = (col0 + 2 * piece) * (int64_t)sizeof(float2);
+            const bool active = piece < npieces;
+            // Half-warp h copies row 2m + h: 16 lanes x 16 B = the row's 256-byte
+            // chunk.  The row pointer comes from its owner lane by shuffle.
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+              if (32 * k >= nrows) break;  // warp-uniform
+#pragma unroll 4
+              for (int m = 0; m < 16; ++m) {
+                const int r = 32 * k + 2 * m + rpar;
+                const unsigned long long base = __shfl_sync(0xffffffffu, myrow[k], (2 * m + rpar) & 31);
+                if (active && r < nrows)
+                  cp_async16(st + stage_off(r, piece), reinterpret_cast<const void*>(base + coff));
+              }
+            }
+            cp_async_arrive(bar);
           }
-          cp_async_arrive(smem_u32(&load_bar[s]));
           issued = gc + 1;
         }
       }
@@ -478,6 +492,8 @@ __global__ void group_single_setup_kernel(GRow* rows, GQuery* query, GHeader* hd
     r.J = J + t * Q;
     r.amax = amax ? amax + t : nullptr;
     for (int c = 0; c < 3; ++c) { r.c_hi[c] = 0.f; r.c_lo[c] = 0.f; }
+    r.tma_row = -1;
+    r.reserved_ = 0;
     rows[t] = r;
   }
   if (t == 0) {
@@ -552,7 +568,7 @@ size_t group_smem_bytes() { return SMEM; }
 int group_threads() { return NTHREADS; }
 int group_reduce_threads() { return RED_THREADS; }
 int group_grid() { return sms(); }
-const void* group_contract_fn(int op, int phase, int tma) { return fn_of(op, phase, tma); }
+const void* group_contract_fn(int op, int phase, int all_tma) { return fn_of(op, phase, all_tma); }
 const void* group_reduce_fn() { return reinterpret_cast<const void*>(group_reduce_kernel); }
 
 int group_prepare_attributes() {
@@ -565,16 +581,17 @@ int group_prepare_attributes() {
   return g_attr_rc;
 }
 
-int launch_group_contract(const GroupDev& g, const CUtensorMap* xmap, int grid, cudaStream_t s) {
+int launch_group_contract(const GroupDev& g, const CUtensorMap* xmap, bool all_tma, int grid, cudaStream_t s) {
   int rc = group_prepare_attributes();
   if (rc) return rc;
   if (g.phase && (g.L <= 0 || g.L > GROUP_MAX_L || g.L % 16 != 0))
     return fail(PI_ERR_UNSUPPORTED, "translation phases need 16 | L <= 512 radial nodes per direction");
+  if ((all_tma || g.tile_tma) && !xmap) return fail(PI_ERR_INVALID_ARGUMENT, "TMA loads need a tensor map");
   CUtensorMap none;
   std::memset(&none, 0, sizeof(none));
   const CUtensorMap& map = xmap ? *xmap : none;
   void* args[2] = {const_cast<GroupDev*>(&g), const_cast<CUtensorMap*>(&map)};
-  PI_CUDA(cudaLaunchKernel(fn_of(g.op, g.phase, xmap != nullptr), dim3(grid), dim3(NTHREADS), args, SMEM, s));
+  PI_CUDA(cudaLaunchKernel(fn_of(g.op, g.phase, all_tma ? 1 : 0), dim3(grid), dim3(NTHREADS), args, SMEM, s));
   count_launch();
   return PI_OK;
 }
@@ -665,7 +682,7 @@ int launch_group_single(const float2* Jw, int64_t Q, int n, int op, double* V, v
   CUtensorMap xmap;
   int rc = encode_row_map(&xmap, Jw, 2 * Q, n);
   if (rc) return rc;
-  rc = launch_group_contract(g, &xmap, std::min(p.items, sms()), s);
+  rc = launch_group_contract(g, &xmap, true, std::min(p.items, sms()), s);
   if (rc) return rc;
   const int64_t red_blocks = std::min<int64_t>(((int64_t)n * n + RED_THREADS - 1) / RED_THREADS, 4 * sms());
   return launch_group_reduce(g, (int)std::max<int64_t>(1, red_blocks), s);

@@ -30,10 +30,13 @@ constexpr int GROUP_MAX_L = 512;       // radial nodes per direction supported b
 
 enum { GROUP_OP_BF16 = 0, GROUP_OP_F16 = 1 };
 
-struct GRow {                          // 40 bytes
+struct GRow {                          // 48 bytes
   const float2* J;                     // ncols complex values, 16-byte aligned
   const float* amax;                   // max |Re|, |Im| over the row (FP16 operands), or null
   float c_hi[3], c_lo[3];              // translation c = c_hi + c_lo
+  int32_t tma_row;                     // first row of a tile whose rows are consecutive rows tma_row,
+                                       // tma_row + 1, ... of the loader's tensor map; -1 otherwise
+  int32_t reserved_;
 };
 
 struct GItem {                         // one work item, derived on the device from the query table
@@ -66,6 +69,8 @@ struct GroupDev {                      // kernel argument; pointers fixed for th
   int64_t ncols;                       // complex columns per row
   int32_t op;                          // GROUP_OP_*
   int32_t phase;                       // 1: rows are direction-major (col = j * L + r) and get e^{i k.c}
+  int32_t tile_tma;                    // gather loader: tiles with rows[first].tma_row >= 0 load by TMA
+  int32_t reserved_;
   int32_t L, M;                        // radial nodes per direction, directions
   const float4* dir_hi;                // directions (double-float), M entries
   const float4* dir_lo;
@@ -89,7 +94,7 @@ __host__ __device__ inline float group_row_scale(float amax) {
 size_t group_smem_bytes();
 int group_threads();
 int group_grid();                      // persistent grid on the current device
-const void* group_contract_fn(int op, int phase, int tma);
+const void* group_contract_fn(int op, int phase, int all_tma);
 const void* group_reduce_fn();
 int group_reduce_threads();
 int group_prepare_attributes();
@@ -127,10 +132,11 @@ __device__ __forceinline__ GItem group_item(const GroupDev& g, int it) {
 // contraction's 128-row x 32-value boxes, 128-byte swizzled.
 int encode_row_map(CUtensorMap* map, const void* base, int64_t row_floats, int64_t n_rows);
 
-// Direct launches (not captured).  xmap != null selects the TMA loader (rows
-// of g.items are then row coordinates of the map); null the cp.async gather
-// through g.rows[].J.
-int launch_group_contract(const GroupDev& g, const CUtensorMap* xmap, int grid, cudaStream_t s);
+// Direct launches (not captured).  all_tma: every tile loads by TMA and row
+// indices are row coordinates of xmap (one query over contiguous rows).
+// Otherwise rows are gathered through g.rows[].J (cp.async), except tiles
+// marked with tma_row when g.tile_tma and xmap are set.
+int launch_group_contract(const GroupDev& g, const CUtensorMap* xmap, bool all_tma, int grid, cudaStream_t s);
 int launch_group_reduce(const GroupDev& g, int grid, cudaStream_t s);
 
 // One query over n contiguous rows Jw + i * Q (the pi_contract layout): the

@@ -26,6 +26,7 @@
 // A query's work items, k-chunk assignment and reduction order depend only on
 // the query itself (its size and the autotuned items-per-SM of its size
 // class), so its result is the same alone and in any mix.
+#include <cuda.h>
 #include <cuda_runtime.h>
 #include <algorithm>
 #include <chrono>
@@ -123,6 +124,7 @@ struct Server {
   Layout lay{};
   // pool
   float2* d_pool = nullptr;
+  CUtensorMap pool_map;          // TMA view of the pool (tiles of consecutive rows load through it)
   float* d_pool_amax = nullptr;  // per pool row: max |Re|, |Im| (sets the FP16 operand scale)
   int64_t pool_rows = 0;
   std::vector<int> row_obj;      // canonical owner, or -1 (free) / -2 (batch-owned)
@@ -249,9 +251,7 @@ int build_graph(Server& S, Slot& sl) {
   cudaGraphNode_t n_commit = nullptr;
   PI_CUDA(cudaGraphAddKernelNode(&n_commit, sl.graph, &sl.n_ff, 1, &cmp));
   // contraction
-  CUtensorMap none_map;
-  std::memset(&none_map, 0, sizeof(none_map));
-  void* con_args[2] = {&sl.g, &none_map};
+  void* con_args[2] = {&sl.g, &S.pool_map};
   cudaKernelNodeParams cpar{};
   cpar.func = const_cast<void*>(group_contract_fn(S.op, 1, 0));
   cpar.gridDim = dim3((unsigned)group_grid());
@@ -293,6 +293,7 @@ int init_slot(Server& S, Slot& sl, int index) {
   g.ncols = S.Qpad;
   g.op = S.op;
   g.phase = 1;
+  g.tile_tma = 1;
   g.L = S.kg->L;
   g.M = S.kg->M;
   g.dir_hi = S.kg->dev.dir_hi;
@@ -415,6 +416,7 @@ int build_batch(Server& S, Slot& sl, std::vector<cudaEvent_t>* waits) {
     // Pass 2: admit.
     S.pending.pop_front();
     const int row0 = sl.n_rows;
+    std::vector<int> qrow(t.n);
     for (int i = 0; i < t.n; ++i) {
       const int o = t.obj[i];
       int r = prow[i];
@@ -466,6 +468,9 @@ int build_batch(Server& S, Slot& sl, std::vector<cudaEvent_t>* waits) {
       GRow& R = rows[sl.n_rows];
       R.J = S.d_pool + (int64_t)r * S.Qpad;
       R.amax = S.d_pool_amax + r;
+      R.tma_row = -1;
+      R.reserved_ = 0;
+      qrow[i] = r;
       // centre c = R o + t
       const double* Rm = &t.rot[9 * i];
       const double* oo = &S.origin[3 * o];
@@ -474,6 +479,13 @@ int build_batch(Server& S, Slot& sl, std::vector<cudaEvent_t>* waits) {
         split_df(cv, &R.c_hi[a], &R.c_lo[a]);
       }
       ++sl.n_rows;
+    }
+    // tiles whose rows are consecutive pool rows load by TMA
+    for (int t0 = 0; t0 < t.n; t0 += GROUP_TILE) {
+      const int na = std::min(GROUP_TILE, t.n - t0);
+      bool run = true;
+      for (int i = 1; i < na && run; ++i) run = qrow[t0 + i] == qrow[t0] + i;
+      if (run) rows[row0 + t0].tma_row = qrow[t0];
     }
     GQuery& q = qs[sl.n_queries];
     q.row0 = row0;
@@ -542,7 +554,7 @@ int launch_batch(Server& S, Slot& sl, const std::vector<cudaEvent_t>& waits) {
     rc = launch_amax_commit(reinterpret_cast<EvalDev*>(sl.d_io + S.lay.evals),
                             &reinterpret_cast<const GHeader*>(sl.d_io + S.lay.hdr)->n_evals, sl.stream);
     if (rc) return rc;
-    rc = launch_group_contract(sl.g, nullptr, group_grid(), sl.stream);
+    rc = launch_group_contract(sl.g, &S.pool_map, false, group_grid(), sl.stream);
     if (rc) return rc;
     rc = launch_group_reduce(sl.g, 4 * S.sms, sl.stream);
     if (rc) return rc;
@@ -702,6 +714,8 @@ int autotune(Server& S) {
       for (int i = 0; i < n * nq; ++i) {
         rw[i].J = S.d_pool + (int64_t)(i % n) * S.Qpad;
         rw[i].amax = S.d_pool_amax + (i % n);
+        rw[i].tma_row = -1;
+        rw[i].reserved_ = 0;
         for (int k = 0; k < 3; ++k) split_df(0.37 * (i % 7) - 0.9 * k, &rw[i].c_hi[k], &rw[i].c_lo[k]);
       }
       for (int j = 0; j < nq; ++j) {
@@ -716,7 +730,7 @@ int autotune(Server& S) {
       for (int rep = 0; rep < 4; ++rep) {
         PI_CUDA(cudaMemsetAsync(sl.d_err, 0, sizeof(int), sl.stream));
         PI_CUDA(cudaEventRecord(a, sl.stream));
-        int rc = launch_group_contract(sl.g, nullptr, group_grid(), sl.stream);
+        int rc = launch_group_contract(sl.g, &S.pool_map, false, group_grid(), sl.stream);
         if (rc) return rc;
         rc = launch_group_reduce(sl.g, 4 * S.sms, sl.stream);
         if (rc) return rc;
@@ -838,6 +852,8 @@ int pi_server_create(pi_kgrid kg, const pi_object* library, int n_library, const
   PI_CUDA(cudaMemset(S->d_pool, 0, (size_t)(S->pool_rows * row_bytes)));
   S->row_obj.assign(S->pool_rows, -1);
   S->row_pin.assign(S->pool_rows, 0);
+  rc = encode_row_map(&S->pool_map, S->d_pool, 2 * S->Qpad, S->pool_rows);
+  if (rc) return rc;
   PI_CUDA(cudaMalloc(reinterpret_cast<void**>(&S->d_pool_amax), (size_t)S->pool_rows * sizeof(float)));
   PI_CUDA(cudaMemset(S->d_pool_amax, 0, (size_t)S->pool_rows * sizeof(float)));
   S->row_slot.assign(S->pool_rows, -1);
