@@ -86,12 +86,15 @@ enum { ERR_LOAD = 1, ERR_CONVERT = 2, ERR_MMA = 3, ERR_EPILOGUE = 4, ERR_CAPACIT
 
 // x[0..31] = 16 complex values of one row, columns col0 .. col0 + 15 of a
 // direction-major row (col = j L + r).  Multiplies them by e^{2 pi i kturn_r (d_j . c)}.
+// sd: the chunk's staged directions (hi, lo of the chunk's first direction,
+// then of the next one), j0 the chunk's first direction.
 __device__ __forceinline__ void apply_phase(float* x, int64_t col0, float3 ch, float3 cl, const GroupDev& g,
-                                            const float2* kt) {
+                                            const float2* kt, const float4* sd, int64_t j0) {
   const int64_t j = col0 / g.L;
   if (j >= g.M) return;  // padding columns hold zeros
   const int r0 = (int)(col0 - j * g.L);
-  const float4 h = g.dir_hi[j], l = g.dir_lo[j];
+  const int slot = j == j0 ? 0 : 2;
+  const float4 h = sd[slot], l = sd[slot + 1];
   const df s = cdot2(make_float3(h.x, h.y, h.z), make_float3(l.x, l.y, l.z), ch, cl);
 #pragma unroll
   for (int i = 0; i < 16; ++i) {
@@ -151,6 +154,7 @@ group_split3_kernel(const GroupDev g, const __grid_constant__ CUtensorMap xmap) 
   __shared__ __align__(8) uint64_t fin_bar;
   __shared__ uint32_t tmem_slot;
   __shared__ float2 kt[PHASE ? GROUP_MAX_L : 1];
+  __shared__ __align__(16) float4 sdir[PHASE ? NST : 1][4];  // per stage: hi, lo of the chunk's (up to) two directions
 
   uint8_t* smem = smem_raw + ((1024 - (smem_u32(smem_raw) & 1023)) & 1023);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -240,6 +244,13 @@ group_split3_kernel(const GroupDev g, const __grid_constant__ CUtensorMap xmap) 
           const int64_t col0 = ((int64_t)w.chunk0 + (int64_t)c * w.cstride) * CK;
           const uint32_t st = smem_u32(smem + s * STAGE) + (uint32_t)(box * BOXB);
           const uint32_t bar = smem_u32(&load_bar[s]);
+          if (PHASE && box == 0 && lane >= 1 && lane <= 4) {
+            // the chunk's directions for the converters' phases (lanes 1-4;
+            // their cp.async arrival below covers these copies)
+            const int64_t j = (col0 + (lane >= 3 ? 16 : 0)) / g.L;
+            if (j < g.M)
+              cp_async16(smem_u32(&sdir[s][lane - 1]), (lane & 1) ? (const void*)(g.dir_hi + j) : (const void*)(g.dir_lo + j));
+          }
           if (tma_row >= 0) {
             // one arrival per lane as in the gather: lane 0's carries the bytes
             if (lane == 0) {
@@ -247,7 +258,7 @@ group_split3_kernel(const GroupDev g, const __grid_constant__ CUtensorMap xmap) 
               tma_load_2d(st, &xmap, (int)(col0 * 2), tma_row, bar);
               tma_load_2d(st + HALF, &xmap, (int)(col0 * 2) + CK, tma_row, bar);
             } else {
-              mbar_arrive(bar);
+              cp_async_arrive(bar);
             }
           } else {
             const int npieces = (int)min((int64_t)CK, g.ncols - col0) / 2;  // 16-byte pieces (2 complex)
@@ -329,12 +340,13 @@ group_split3_kernel(const GroupDev g, const __grid_constant__ CUtensorMap xmap) 
           for (int i = 0; i < 16; ++i)
             if (i >= nvalid) { xa[2 * i] = xa[2 * i + 1] = 0.f; xb[2 * i] = xb[2 * i + 1] = 0.f; }
         }
+        const int64_t j0 = (((int64_t)w.chunk0 + (int64_t)c * w.cstride) * CK) / (PHASE ? g.L : 1);
         if (va) {
-          if (PHASE) apply_phase(xa, col0, cah, cal, g, kt);
+          if (PHASE) apply_phase(xa, col0, cah, cal, g, kt, sdir[PHASE ? s : 0], j0);
           store_split<OP>(st, row, h, xa, sa);
         }
         if (vb) {
-          if (PHASE) apply_phase(xb, col0, cbh, cbl, g, kt);
+          if (PHASE) apply_phase(xb, col0, cbh, cbl, g, kt, sdir[PHASE ? s : 0], j0);
           store_split<OP>(st + 2 * OPB, row, h, xb, sb);
         }
         fence_proxy_async();
