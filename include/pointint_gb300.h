@@ -229,6 +229,34 @@ int pi_pair_volume_grad_host(const pi_object* o1, const pi_object* o2, const dou
  * at offset n * sum_{m<i} n_dofs[m] + j * n_dofs[i]. */
 int pi_volume_matrix_grad_host(const pi_object* objs, int n_objects, const double* dirs, const double* kmag,
                                const double* w, int64_t Q, double* V_out, double* grad_out);
+/* ---- Gauss-Newton Hessian -------------------------------------------------------- */
+/* DoF Jacobian of the form factors: d_G[d][q] = sqrt(|w_q|) dA_n(k_q)/dtheta_{n,d},
+ * rows in the order of the concatenated DoF vector (12 per AffineDoF object,
+ * 3V per TriangleMeshDoF object; pi_batch_layout gives each object's first
+ * row), Q complex64 per row, the object's position phase included.  This is
+ * the reference's per-k dA/dtheta (compute_A_gradient, affine_dof.cpp:172-322,
+ * triangle_mesh_dof.cpp:76-143; K4/K5/K8 cpp/src/dof/cuda/affine_dof_cuda.cu:254-576,
+ * cpp/src/dof/cuda/triangle_mesh_dof_cuda.cu:147-310) in the contraction's
+ * operand form: the Gauss-Newton Hessian blocks are Re(G_i diag(sign w) G_j^H)/(8 pi^3),
+ * which pi_contract forms from the stacked rows. */
+int pi_dof_jacobian(pi_kgrid kg, pi_batch b, void* d_G, pi_stream stream);
+/* compute_intersection_volume_matrix_cuda with GRADIENT | HESSIAN
+ * (cpp/include/compute_intersection_volume_multi_object.hpp:21-59;
+ * hessian_ij, cpp/src/compute_intersection_volume_multi_object.cu:189-229):
+ * V (n x n), grad_out (may be NULL; packed as in pi_volume_matrix_grad_host)
+ * and hess_out = hessian_ij[i][j] for every (i, j): blocks of n_dofs[i] x n_dofs[j]
+ * doubles (row-major) in (i, j) row-major order.  hessian_ii and hessian_jj
+ * are zero in the reference's Gauss-Newton form and are not returned. */
+int pi_volume_matrix_hessian_host(const pi_object* objs, int n_objects, const double* dirs, const double* kmag,
+                                  const double* w, int64_t Q, double* V_out, double* grad_out, double* hess_out);
+/* compute_intersection_volume_cuda with GRADIENT | HESSIAN
+ * (cpp/include/compute_intersection_volume.hpp:24-59; K11,
+ * cpp/src/compute_intersection_volume.cu:109-157): volume, grad_geom1/2 (may be
+ * NULL), hessian_geom1 (d1 x d1), hessian_geom2 (d2 x d2), hessian_cross (d1 x d2). */
+int pi_pair_volume_hessian_host(const pi_object* o1, const pi_object* o2, const double* dirs, const double* kmag,
+                                const double* w, int64_t Q, double* volume, double* grad1, double* grad2,
+                                double* H11, double* H22, double* H12);
+
 /* CudaComputeAkFunc registry plugin (cpp/include/dof/cuda/dof_cuda_interface.hpp:24-30):
  * host object and k-grid, output d_A_out = Q complex doubles (double2) on the device. */
 int pi_compute_Ak(const pi_object* obj, const double* dirs, const double* kmag, int64_t Q, double* d_A_out,

@@ -106,6 +106,9 @@ SIGNATURES = {
     "pi_dof_gradients": (I32, [P, P, P, P, P, P, SZ, P]),
     "pi_pair_volume_grad_host": (I32, [OBJP, OBJP, P, P, P, I64, ctypes.POINTER(D), P, P]),
     "pi_volume_matrix_grad_host": (I32, [OBJP, I32, P, P, P, I64, P, P]),
+    "pi_dof_jacobian": (I32, [P, P, P, P]),
+    "pi_volume_matrix_hessian_host": (I32, [OBJP, I32, P, P, P, I64, P, P, P]),
+    "pi_pair_volume_hessian_host": (I32, [OBJP, OBJP, P, P, P, I64, ctypes.POINTER(D), P, P, P, P, P]),
     "pi_volume_matrix_host": (I32, [OBJP, I32, P, P, P, I64, I32, I32, P]),
     "pi_pair_volume_host": (I32, [OBJP, OBJP, P, P, P, I64, ctypes.POINTER(D)]),
     "pi_compute_Ak": (I32, [OBJP, P, P, I64, P, I32]),

@@ -232,6 +232,63 @@ def volume_matrix_grad_host(kgrid: KGrid, objects: list[SceneObject]):
     return V, grad
 
 
+# ----------------------------------------------------------------------------- Gauss-Newton Hessian
+def dof_jacobian(kgrid: KGrid, batch: ObjectBatch, out: torch.Tensor | None = None, stream=None) -> torch.Tensor:
+    """G[d, q] = sqrt|w_q| dA(k_q)/dtheta_d over the concatenated DoF vector
+    (complex64 [D, Q] on the device).  contract(kgrid, G) is the full
+    Gauss-Newton Hessian; contract of the stack [J; G] adds V and dV/dtheta."""
+    D = sum(len(o.dofs) for o in batch.objects)
+    Q = kgrid.num_nodes
+    if out is None:
+        out = torch.empty((D, Q), dtype=torch.complex64, device="cuda")
+    if out.shape != (D, Q) or out.dtype != torch.complex64 or not out.is_contiguous():
+        raise ValueError("out must be a contiguous complex64 tensor of shape (n_dofs_total, Q)")
+    _lib.check(_lib.lib().pi_dof_jacobian(kgrid.handle(), batch.handle, ctypes.c_void_p(out.data_ptr()),
+                                          _stream(stream)))
+    return out
+
+
+def volume_matrix_hessian_host(kgrid: KGrid, objects: list[SceneObject]):
+    """Reference compute_intersection_volume_matrix_cuda(..., GRADIENT | HESSIAN):
+    (V, grad, hess) with grad[i][j] = dV_ij/dtheta_i and hess[i][j] the
+    Gauss-Newton block hessian_ij (n_dofs[i] x n_dofs[j])."""
+    n = len(objects)
+    nd = [len(o.dofs) for o in objects]
+    V = np.zeros((n, n))
+    g = np.zeros(max(1, n * sum(nd)))
+    h = np.zeros(max(1, sum(a * b for a in nd for b in nd)))
+    arr = (_lib.PiObject * n)(*[o.as_c() for o in objects])
+    _lib.check(_lib.lib().pi_volume_matrix_hessian_host(arr, n, kgrid.dirs.ctypes.data, kgrid.kmag.ctypes.data,
+                                                        kgrid.w.ctypes.data, kgrid.num_nodes, V.ctypes.data,
+                                                        g.ctypes.data, h.ctypes.data))
+    grad, off = [], 0
+    for i in range(n):
+        grad.append([g[off + j * nd[i]: off + (j + 1) * nd[i]].copy() for j in range(n)])
+        off += n * nd[i]
+    hess, off = [[None] * n for _ in range(n)], 0
+    for i in range(n):
+        for j in range(n):
+            hess[i][j] = h[off: off + nd[i] * nd[j]].reshape(nd[i], nd[j]).copy()
+            off += nd[i] * nd[j]
+    return V, grad, hess
+
+
+def pair_volume_hessian_host(kgrid: KGrid, o1: SceneObject, o2: SceneObject) -> dict:
+    """Reference compute_intersection_volume_cuda(..., GRADIENT | HESSIAN) as a
+    dict with the reference's result field names."""
+    c1, c2 = o1.as_c(), o2.as_c()
+    d1, d2 = len(o1.dofs), len(o2.dofs)
+    v = ctypes.c_double(0.0)
+    g1, g2 = np.zeros(d1), np.zeros(d2)
+    H11, H22, H12 = np.zeros((d1, d1)), np.zeros((d2, d2)), np.zeros((d1, d2))
+    _lib.check(_lib.lib().pi_pair_volume_hessian_host(ctypes.byref(c1), ctypes.byref(c2), kgrid.dirs.ctypes.data,
+                                                      kgrid.kmag.ctypes.data, kgrid.w.ctypes.data, kgrid.num_nodes,
+                                                      ctypes.byref(v), g1.ctypes.data, g2.ctypes.data,
+                                                      H11.ctypes.data, H22.ctypes.data, H12.ctypes.data))
+    return {"volume": float(v.value), "grad_geom1": g1, "grad_geom2": g2, "hessian_geom1": H11,
+            "hessian_geom2": H22, "hessian_cross": H12}
+
+
 class _DofVolumeFn(torch.autograd.Function):
     """V(theta) for all DoFs theta (concatenated), backward through the adjoint."""
 

@@ -526,6 +526,98 @@ int pi_volume_matrix_grad_host(const pi_object* objs, int n, const double* dirs,
   return PI_OK;
 }
 
+int pi_dof_jacobian(pi_kgrid kg, pi_batch b, void* d_G, pi_stream stream) {
+  if (!kg || !b || (!d_G && dof_gradient_size(b) > 0)) return fail(PI_ERR_INVALID_ARGUMENT, "pi_dof_jacobian: bad arguments");
+  return launch_jacobian(kg, b, static_cast<float2*>(d_G), reinterpret_cast<cudaStream_t>(stream));
+}
+
+// Shared body of the Hessian drop-ins.  X = [J; G] (n + D rows of sqrt|w|-scaled
+// form factors and DoF Jacobian rows) and one FP32 contraction
+// Re(X diag(sign w) X^H)/(8 pi^3) give, in its blocks, V (rows and columns
+// < n), dV_ij/dtheta_i (row n + goff_i + a, column j) and the Gauss-Newton
+// Hessian (rows and columns >= n).  Returns the full (n + D)^2 matrix on the host.
+static int stacked_gram_host(const pi_object* objs, int n, const double* dirs, const double* kmag, const double* w,
+                             int64_t Q, std::vector<double>* X, int64_t* D_out) {
+  cudaStream_t s = cudaStreamPerThread;
+  KGridGuard kg;
+  int rc = pi_kgrid_create(dirs, kmag, w, Q, &kg.k);
+  if (rc) return rc;
+  BatchGuard b;
+  rc = pi_batch_create(objs, n, 0, reinterpret_cast<pi_stream>(s), &b.b);
+  if (rc) return rc;
+  const int64_t D = dof_gradient_size(b.b), m = n + D;
+  if (m > INT32_MAX) return fail(PI_ERR_UNSUPPORTED, "too many DoFs for the Hessian");
+  size_t ws_bytes = 0;
+  if ((rc = pi_contract_workspace_size(kg.k, (int)m, PI_CONTRACT_FP32, &ws_bytes))) return rc;
+  DevBuf J, ws, H;
+  if ((rc = J.alloc((size_t)m * Q * sizeof(float2), s)) || (rc = ws.alloc(ws_bytes, s)) ||
+      (rc = H.alloc((size_t)m * m * sizeof(double), s)))
+    return rc;
+  float2* Jp = static_cast<float2*>(J.p);
+  if ((rc = pi_form_factors(kg.k, b.b, 1, Jp, reinterpret_cast<pi_stream>(s)))) return rc;
+  if ((rc = launch_jacobian(kg.k, b.b, Jp + (size_t)n * Q, s))) return rc;
+  if ((rc = pi_contract(kg.k, Jp, (int)m, PI_CONTRACT_FP32, static_cast<double*>(H.p), ws.p, ws_bytes,
+                        reinterpret_cast<pi_stream>(s))))
+    return rc;
+  X->resize((size_t)m * m);
+  PI_CUDA(cudaMemcpyAsync(X->data(), H.p, (size_t)m * m * sizeof(double), cudaMemcpyDeviceToHost, s));
+  PI_CUDA(cudaStreamSynchronize(s));
+  *D_out = D;
+  return PI_OK;
+}
+
+int pi_volume_matrix_hessian_host(const pi_object* objs, int n, const double* dirs, const double* kmag,
+                                  const double* w, int64_t Q, double* V_out, double* grad_out, double* hess_out) {
+  if (n <= 0 || !objs || !V_out || !hess_out || !dirs || !kmag || !w)
+    return fail(PI_ERR_INVALID_ARGUMENT, "pi_volume_matrix_hessian_host: bad arguments");
+  std::vector<double> X;
+  int64_t D = 0;
+  int rc = stacked_gram_host(objs, n, dirs, kmag, w, Q, &X, &D);
+  if (rc) return rc;
+  const int64_t m = n + D;
+  std::vector<int64_t> goff(n + 1, 0);
+  for (int i = 0; i < n; ++i) goff[i + 1] = goff[i] + objs[i].n_dofs;
+  for (int i = 0; i < n; ++i)
+    for (int j = 0; j < n; ++j) V_out[(size_t)i * n + j] = X[(size_t)i * m + j];
+  if (grad_out)  // block (i, j) = dV_ij/dtheta_i at n * goff_i + j * d_i
+    for (int i = 0; i < n; ++i)
+      for (int j = 0; j < n; ++j)
+        for (int64_t a = 0; a < objs[i].n_dofs; ++a)
+          grad_out[n * goff[i] + j * objs[i].n_dofs + a] = X[(size_t)(n + goff[i] + a) * m + j];
+  // hessian_ij blocks in (i, j) row-major order, each d_i x d_j row-major
+  size_t off = 0;
+  for (int i = 0; i < n; ++i)
+    for (int j = 0; j < n; ++j)
+      for (int64_t a = 0; a < objs[i].n_dofs; ++a)
+        for (int64_t c = 0; c < objs[j].n_dofs; ++c) hess_out[off++] = X[(size_t)(n + goff[i] + a) * m + n + goff[j] + c];
+  return PI_OK;
+}
+
+int pi_pair_volume_hessian_host(const pi_object* o1, const pi_object* o2, const double* dirs, const double* kmag,
+                                const double* w, int64_t Q, double* volume, double* grad1, double* grad2, double* H11,
+                                double* H22, double* H12) {
+  if (!o1 || !o2 || !volume || !H11 || !H22 || !H12)
+    return fail(PI_ERR_INVALID_ARGUMENT, "pi_pair_volume_hessian_host: bad arguments");
+  pi_object objs[2] = {*o1, *o2};
+  std::vector<double> X;
+  int64_t D = 0;
+  int rc = stacked_gram_host(objs, 2, dirs, kmag, w, Q, &X, &D);
+  if (rc) return rc;
+  const int64_t m = 2 + D, d1 = o1->n_dofs, d2 = o2->n_dofs;
+  auto at = [&](int64_t r, int64_t c) { return X[(size_t)r * m + c]; };
+  *volume = at(0, 1);
+  for (int64_t a = 0; a < d1; ++a) {
+    if (grad1) grad1[a] = at(2 + a, 1);  // dV_12/dtheta_1: G_1 rows against A_2
+    for (int64_t c = 0; c < d1; ++c) H11[a * d1 + c] = at(2 + a, 2 + c);
+    for (int64_t c = 0; c < d2; ++c) H12[a * d2 + c] = at(2 + a, 2 + d1 + c);
+  }
+  for (int64_t a = 0; a < d2; ++a) {
+    if (grad2) grad2[a] = at(2 + d1 + a, 0);
+    for (int64_t c = 0; c < d2; ++c) H22[a * d2 + c] = at(2 + d1 + a, 2 + d1 + c);
+  }
+  return PI_OK;
+}
+
 int pi_compute_Ak(const pi_object* obj, const double* dirs, const double* kmag, int64_t Q, double* d_A_out,
                   int block_size) {
   (void)block_size;  // kept for signature parity with CudaComputeAkFunc; the kernel picks its own shape

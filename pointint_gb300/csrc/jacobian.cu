@@ -1,0 +1,419 @@
+// Jacobian of the form factors with respect to the DoFs, and from it the
+// Gauss-Newton Hessian blocks.
+//
+//   G[d][q] = sqrt|w_q| dA_n(k_q)/dtheta_{n,d}
+//
+// for every object n and DoF d, rows in the order of the concatenated DoF
+// vector, FP32 complex, q-major like J.  The reference's Gauss-Newton blocks
+// (hessian_ij of compute_intersection_volume_multi_object.cpp:236-292 / K16
+// cpp/src/compute_intersection_volume_multi_object.cu:189-229; hessian_geom1,
+// geom2, cross of compute_intersection_volume_cpu.cpp:153-186 / K11
+// cpp/src/compute_intersection_volume.cu:109-157) are blocks of
+//
+//   H = Re(G diag(sign w) G^H) / (8 pi^3),
+//
+// which the volume contraction forms from G's rows exactly as it forms V from
+// J's.  The per-element derivatives are the adjoint's (adjoint.cu); here they
+// are summed over elements at every k-node (forward mode) instead of over
+// k-nodes for every element.
+//
+//  * AffineDoF triangles (x = A x0 + t): dA/dt_r = i k_r A; dA/dA_rc =
+//    sum_e sum_s (df_e/dv_s)_r x0_{s,c} with df/dv_s = -2 (c_s F + gamma k d D_s),
+//    so each thread accumulates sum_e F U_e (U_rc = sum_s c_{s,r} x0_{s,c}) and
+//    sum_e gamma sum_s D_s x0_s.
+//  * AffineDoF disks / Gaussians (c = A c0 + t, n' = A n0, M = A A^T):
+//    dA/dA_rc = i k d_r Z_c + khat_r N_c + k^2 d_r (A^T d)_c Y with
+//    Z = sum P S a c0, N = sum P (S - k^2 s_n^2 S_r) n0, Y = sum P a S_r.
+//  * TriangleMeshDoF: dA/dv_p = sum over the triangles at vertex p of
+//    df_e/dv_p (a gather over the batch's vertex adjacency, no atomics).
+//
+// Thread layout as ff_kernel with one radius per thread: a warp owns 32
+// directions at one radius; the origin phase e^{ik.o} and sqrt|w| are applied
+// once per output.
+#include <cuda_runtime.h>
+#include <algorithm>
+#include <cstdint>
+#include <vector>
+#include "pi_internal.h"
+#include "dfmath.cuh"
+#include "bessel.cuh"
+#include "tri_adjoint.cuh"
+
+namespace pi {
+
+namespace {
+
+constexpr int JAC_THREADS = 128;
+constexpr int JAC_WARPS = JAC_THREADS / 32;
+constexpr int JAC_TILE = 128;
+
+enum { JAC_AFFINE_TRI = 0, JAC_AFFINE_SURF = 1, JAC_MESH_TRI = 2 };
+
+struct JacObj {
+  int32_t obj, kind;
+  int64_t row0;                    // first row of G
+  int64_t vstart, nverts;          // TriangleMeshDoF: vertex range in the batch's adjacency
+  const unsigned char* src;        // reference-layout source elements
+  const double* dofs;              // device DoF vector
+};
+
+struct TriSrcJ { double a[3], e1[3], e2[3], S[3]; int32_t vid0, vid1, vid2, pad; };
+struct SurfSrcJ { double c[3], n[3], p0, p1; };
+
+// FP32 sum with chunked partials and a compensated running total (complex).
+struct kcf {
+  float pr = 0.f, pi = 0.f, sr = 0.f, si = 0.f, cr = 0.f, ci = 0.f;
+  __device__ __forceinline__ void add(float re, float im) { pr += re; pi += im; }
+  __device__ __forceinline__ void fma_add(cf a, float s) { pr = fmaf(a.re, s, pr); pi = fmaf(a.im, s, pi); }
+  __device__ __forceinline__ void flush() {
+    float y = pr - cr, t = sr + y;
+    cr = (t - sr) - y; sr = t;
+    y = pi - ci; t = si + y;
+    ci = (t - si) - y; si = t;
+    pr = pi = 0.f;
+  }
+  __device__ __forceinline__ cf value() const { return cf{sr, si}; }
+};
+
+struct JacThread {
+  int j, r;
+  bool active;
+  float3 dh, dl;
+  float inv_norm, dnorm;
+  df k;
+};
+
+__device__ __forceinline__ JacThread jac_thread(const KGridDev& kg) {
+  JacThread t;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int item = blockIdx.x * JAC_WARPS + warp;
+  const int dt = item / kg.L;
+  t.r = item - dt * kg.L;
+  t.j = dt * 32 + lane;
+  t.active = dt < (kg.M + 31) / 32 && t.j < kg.M;
+  t.dh = t.dl = make_float3(0.f, 0.f, 0.f);
+  t.inv_norm = t.dnorm = 0.f;
+  t.k = df{0.f, 0.f};
+  if (t.active) {
+    const float4 h = kg.dir_hi[t.j], l = kg.dir_lo[t.j];
+    t.dh = make_float3(h.x, h.y, h.z);
+    t.dl = make_float3(l.x, l.y, l.z);
+    t.inv_norm = h.w;
+    t.dnorm = l.w;
+    const float2 km = kg.kmag[t.r];
+    t.k = df{km.x, km.y};
+  }
+  return t;
+}
+
+// e^{ik.o} sqrt|w| for this thread's node (0 at k = 0, where A = 0 by definition).
+__device__ __forceinline__ cf jac_out_scale(const JacThread& t, const KGridDev& kg, const ObjDev& od, int64_t q) {
+  const double so_d = ((double)t.dh.x + t.dl.x) * od.origin[0] + ((double)t.dh.y + t.dl.y) * od.origin[1] +
+                      ((double)t.dh.z + t.dl.z) * od.origin[2];
+  const float so_h = (float)so_d;
+  const cf e = cis(df_mul(t.k, df{so_h, (float)(so_d - (double)so_h)}));
+  const float s = (t.k.hi * t.dnorm < 1e-10f) ? 0.f : kg.sqrtw[q];
+  return cf{e.re * s, e.im * s};
+}
+
+// Triangle derivative pieces at one node: F, D_a, D_b, D_c (tri_adjoint.cuh),
+// gamma = khat.S and the gradient vectors c_s of gamma with respect to the vertices.
+struct TriNode {
+  TriDer d;
+  float gam;
+  float3 c[3];
+};
+
+__device__ __forceinline__ TriNode tri_node(const JacThread& t, float3 m, float3 e1, float3 e2, float3 S) {
+  TriNode o;
+  const df sm = cdot(t.dh, t.dl, m), d1 = cdot(t.dh, t.dl, e1), d2 = cdot(t.dh, t.dl, e2);
+  const float sp = fmaxf(fmaxf(fabsf(d1.hi), fabsf(d2.hi)), fabsf(d2.hi - d1.hi));
+  const float al = t.k.hi * d1.hi, be = t.k.hi * d2.hi;
+  if (t.k.hi * sp < 2.0f) {
+    o.d = tri_series_der(cis(df_mul_un(t.k, sm)), al, be);
+  } else {
+    const df sa = df_add(sm, df_div3(df_add(d1, d2)) * -1.0f);
+    const df sb = df_add(sa, d1), sc = df_add(sa, d2);
+    o.d = tri_generic_der(cis(df_mul_un(t.k, sa)), cis(df_mul_un(t.k, sb)), cis(df_mul_un(t.k, sc)), al, be);
+  }
+  o.gam = (t.dh.x * S.x + t.dh.y * S.y + t.dh.z * S.z) * t.inv_norm;
+  const float3 kh = make_float3(t.dh.x * t.inv_norm, t.dh.y * t.inv_norm, t.dh.z * t.inv_norm);
+  const float3 w0 = make_float3(e2.x - e1.x, e2.y - e1.y, e2.z - e1.z);
+  o.c[0] = make_float3(0.5f * (kh.y * w0.z - kh.z * w0.y), 0.5f * (kh.z * w0.x - kh.x * w0.z),
+                       0.5f * (kh.x * w0.y - kh.y * w0.x));
+  o.c[1] = make_float3(-0.5f * (kh.y * e2.z - kh.z * e2.y), -0.5f * (kh.z * e2.x - kh.x * e2.z),
+                       -0.5f * (kh.x * e2.y - kh.y * e2.x));
+  o.c[2] = make_float3(0.5f * (kh.y * e1.z - kh.z * e1.y), 0.5f * (kh.z * e1.x - kh.x * e1.z),
+                       0.5f * (kh.x * e1.y - kh.y * e1.x));
+  return o;
+}
+
+__device__ __forceinline__ float comp(float3 v, int i) { return i == 0 ? v.x : (i == 1 ? v.y : v.z); }
+
+// ---- AffineDoF triangles -------------------------------------------------------------
+__global__ void __launch_bounds__(JAC_THREADS)
+jac_affine_tri_kernel(KGridDev kg, BatchDev b, const JacObj* __restrict__ jobs, float2* __restrict__ G) {
+  const JacObj jo = jobs[blockIdx.y];
+  const ObjDev od = b.objs[jo.obj];
+  const JacThread t = jac_thread(kg);
+  __shared__ float4 tile[6 * JAC_TILE];
+  kcf A, MF[9], W[3];
+  const float4* pool = b.tri_pool + 3 * od.elem_off;
+  const TriSrcJ* src = reinterpret_cast<const TriSrcJ*>(jo.src);
+  for (int base = 0; base < od.n_elems; base += JAC_TILE) {
+    const int cnt = min(JAC_TILE, od.n_elems - base);
+    __syncthreads();
+    for (int e = threadIdx.x; e < cnt; e += JAC_THREADS) {
+      tile[6 * e] = pool[3 * (int64_t)(base + e)];
+      tile[6 * e + 1] = pool[3 * (int64_t)(base + e) + 1];
+      tile[6 * e + 2] = pool[3 * (int64_t)(base + e) + 2];
+      const TriSrcJ& s = src[base + e];  // reference positions x0 of the three vertices
+      tile[6 * e + 3] = make_float4((float)s.a[0], (float)s.a[1], (float)s.a[2], 0.f);
+      tile[6 * e + 4] = make_float4((float)(s.a[0] + s.e1[0]), (float)(s.a[1] + s.e1[1]), (float)(s.a[2] + s.e1[2]), 0.f);
+      tile[6 * e + 5] = make_float4((float)(s.a[0] + s.e2[0]), (float)(s.a[1] + s.e2[1]), (float)(s.a[2] + s.e2[2]), 0.f);
+    }
+    __syncthreads();
+    if (!t.active) continue;
+    for (int e = 0; e < cnt; ++e) {
+      const float4 q0 = tile[6 * e], q1 = tile[6 * e + 1], q2 = tile[6 * e + 2];
+      const float3 x0[3] = {make_float3(tile[6 * e + 3].x, tile[6 * e + 3].y, tile[6 * e + 3].z),
+                            make_float3(tile[6 * e + 4].x, tile[6 * e + 4].y, tile[6 * e + 4].z),
+                            make_float3(tile[6 * e + 5].x, tile[6 * e + 5].y, tile[6 * e + 5].z)};
+      const TriNode o = tri_node(t, make_float3(q0.x, q0.y, q0.z), make_float3(q1.x, q1.y, q1.z),
+                                 make_float3(q2.x, q2.y, q2.z), make_float3(q0.w, q1.w, q2.w));
+      A.fma_add(o.d.F, -2.0f * o.gam);
+      const cf Ds[3] = {o.d.Da, o.d.Db, o.d.Dc};
+#pragma unroll
+      for (int r = 0; r < 3; ++r)
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+          const float U = comp(o.c[0], r) * comp(x0[0], c) + comp(o.c[1], r) * comp(x0[1], c) +
+                          comp(o.c[2], r) * comp(x0[2], c);
+          MF[3 * r + c].fma_add(o.d.F, U);
+        }
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        const float w0 = o.gam * comp(x0[0], c), w1 = o.gam * comp(x0[1], c), w2 = o.gam * comp(x0[2], c);
+        W[c].add(Ds[0].re * w0 + Ds[1].re * w1 + Ds[2].re * w2, Ds[0].im * w0 + Ds[1].im * w1 + Ds[2].im * w2);
+      }
+      if ((e & 15) == 15) {
+        A.flush();
+#pragma unroll
+        for (int a = 0; a < 9; ++a) MF[a].flush();
+#pragma unroll
+        for (int a = 0; a < 3; ++a) W[a].flush();
+      }
+    }
+    A.flush();
+#pragma unroll
+    for (int a = 0; a < 9; ++a) MF[a].flush();
+#pragma unroll
+    for (int a = 0; a < 3; ++a) W[a].flush();
+  }
+  if (!t.active) return;
+  const int64_t q = (int64_t)t.r * kg.M + t.j;
+  const cf sc = jac_out_scale(t, kg, od, q);
+  const float k = t.k.hi;
+  const cf a = cmul(A.value(), sc);
+  float2* out = G + jo.row0 * kg.Q + q;
+#pragma unroll
+  for (int r = 0; r < 3; ++r) {  // dA/dt_r = i k d_r A
+    const float kr = k * comp(t.dh, r);
+    out[(int64_t)r * kg.Q] = make_float2(-kr * a.im, kr * a.re);
+  }
+#pragma unroll
+  for (int r = 0; r < 3; ++r)
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      const cf mf = MF[3 * r + c].value(), w = W[c].value();
+      const float kd = k * comp(t.dh, r);
+      const cf v = cmul(cf{-2.0f * (mf.re + kd * w.re), -2.0f * (mf.im + kd * w.im)}, sc);
+      out[(int64_t)(3 + 3 * r + c) * kg.Q] = make_float2(v.re, v.im);
+    }
+}
+
+// ---- AffineDoF disks / Gaussians --------------------------------------------------------
+__global__ void __launch_bounds__(JAC_THREADS)
+jac_affine_surf_kernel(KGridDev kg, BatchDev b, const JacObj* __restrict__ jobs, float2* __restrict__ G) {
+  const JacObj jo = jobs[blockIdx.y];
+  const ObjDev od = b.objs[jo.obj];
+  const JacThread t = jac_thread(kg);
+  const bool disk = od.type == PI_GEOM_DISK;
+  __shared__ float4 tile[4 * JAC_TILE];
+  const float* Ms = od.Msym;
+  const float qd = t.dh.x * (Ms[0] * t.dh.x + Ms[1] * t.dh.y + Ms[2] * t.dh.z) +
+                   t.dh.y * (Ms[1] * t.dh.x + Ms[3] * t.dh.y + Ms[4] * t.dh.z) +
+                   t.dh.z * (Ms[2] * t.dh.x + Ms[4] * t.dh.y + Ms[5] * t.dh.z);
+  kcf A, Z[3], N[3], Y;
+  const float4* pool = b.surf_pool + 2 * od.elem_off;
+  const SurfSrcJ* src = reinterpret_cast<const SurfSrcJ*>(jo.src);
+  const float k = t.k.hi, k2 = k * k;
+  for (int base = 0; base < od.n_elems; base += JAC_TILE) {
+    const int cnt = min(JAC_TILE, od.n_elems - base);
+    __syncthreads();
+    for (int e = threadIdx.x; e < cnt; e += JAC_THREADS) {
+      tile[4 * e] = pool[2 * (int64_t)(base + e)];
+      tile[4 * e + 1] = pool[2 * (int64_t)(base + e) + 1];
+      const SurfSrcJ& s = src[base + e];  // reference centre c0 and normal n0
+      tile[4 * e + 2] = make_float4((float)s.c[0], (float)s.c[1], (float)s.c[2], 0.f);
+      tile[4 * e + 3] = make_float4((float)s.n[0], (float)s.n[1], (float)s.n[2], 0.f);
+    }
+    __syncthreads();
+    if (!t.active) continue;
+    for (int e = 0; e < cnt; ++e) {
+      const float4 q0 = tile[4 * e], q1 = tile[4 * e + 1], c0 = tile[4 * e + 2], n0 = tile[4 * e + 3];
+      const df sc = cdot(t.dh, t.dl, make_float3(q0.x, q0.y, q0.z));
+      const float sn = t.dh.x * q1.x + t.dh.y * q1.y + t.dh.z * q1.z;
+      const float perp = fmaxf(qd - sn * sn, 0.f);
+      const float amp = sn * t.inv_norm;
+      const cf P = cis(df_mul_un(t.k, sc));
+      float S, Sr;
+      if (disk) {
+        const float x = k * q0.w * sqrtf(perp);
+        S = q1.w * ((x < 1e-10f) ? 1.0f : 2.0f * j1x(x));
+        Sr = -2.0f * q1.w * q0.w * q0.w * j2x2(x);
+      } else {
+        S = q1.w * __expf(-0.5f * q0.w * q0.w * k2 * perp);
+        Sr = -q0.w * q0.w * S;
+      }
+      const float sa = S * amp, sn_t = S - k2 * sn * sn * Sr;
+      A.fma_add(P, sa);
+      Z[0].fma_add(P, sa * c0.x); Z[1].fma_add(P, sa * c0.y); Z[2].fma_add(P, sa * c0.z);
+      N[0].fma_add(P, sn_t * n0.x); N[1].fma_add(P, sn_t * n0.y); N[2].fma_add(P, sn_t * n0.z);
+      Y.fma_add(P, amp * Sr);
+      if ((e & 15) == 15) {
+        A.flush(); Y.flush();
+#pragma unroll
+        for (int a = 0; a < 3; ++a) { Z[a].flush(); N[a].flush(); }
+      }
+    }
+    A.flush(); Y.flush();
+#pragma unroll
+    for (int a = 0; a < 3; ++a) { Z[a].flush(); N[a].flush(); }
+  }
+  if (!t.active) return;
+  const int64_t q = (int64_t)t.r * kg.M + t.j;
+  const cf scl = jac_out_scale(t, kg, od, q);
+  const double* Am = jo.dofs + 3;  // A row-major
+  float atd[3];  // (A^T d)_c = sum_p d_p A_pc
+#pragma unroll
+  for (int c = 0; c < 3; ++c)
+    atd[c] = (float)(t.dh.x * Am[c] + t.dh.y * Am[3 + c] + t.dh.z * Am[6 + c]);
+  const cf a = cmul(A.value(), scl), y = Y.value();
+  float2* out = G + jo.row0 * kg.Q + q;
+#pragma unroll
+  for (int r = 0; r < 3; ++r) {
+    const float kr = k * comp(t.dh, r);
+    out[(int64_t)r * kg.Q] = make_float2(-kr * a.im, kr * a.re);
+  }
+#pragma unroll
+  for (int r = 0; r < 3; ++r)
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      const float dr = comp(t.dh, r);
+      const cf z = Z[c].value(), nn = N[c].value();
+      // i k d_r Z_c + khat_r N_c + k^2 d_r (A^T d)_c Y
+      const float f = k2 * dr * atd[c], g = dr * t.inv_norm, kd = k * dr;
+      const cf v = cmul(cf{-kd * z.im + g * nn.re + f * y.re, kd * z.re + g * nn.im + f * y.im}, scl);
+      out[(int64_t)(3 + 3 * r + c) * kg.Q] = make_float2(v.re, v.im);
+    }
+}
+
+// ---- TriangleMeshDoF: vertex gather --------------------------------------------------------
+__global__ void __launch_bounds__(JAC_THREADS)
+jac_mesh_kernel(KGridDev kg, BatchDev b, const JacObj* __restrict__ jobs, const int64_t* __restrict__ vrow,
+                const int64_t* __restrict__ vent, const int64_t* __restrict__ vmap, float2* __restrict__ G) {
+  const JacObj jo = jobs[blockIdx.y];
+  const ObjDev od = b.objs[jo.obj];
+  const JacThread t = jac_thread(kg);
+  if (!t.active) return;
+  const int64_t q = (int64_t)t.r * kg.M + t.j;
+  const cf scl = jac_out_scale(t, kg, od, q);
+  const float k = t.k.hi;
+  for (int64_t v = jo.vstart; v < jo.vstart + jo.nverts; ++v) {
+    float gr[3] = {0.f, 0.f, 0.f}, gi[3] = {0.f, 0.f, 0.f};
+    for (int64_t p = vrow[v]; p < vrow[v + 1]; ++p) {
+      const int64_t te = vent[p];  // pool triangle * 3 + slot
+      const int64_t tri = te / 3;
+      const int slot = (int)(te - 3 * tri);
+      const float4 q0 = b.tri_pool[3 * tri], q1 = b.tri_pool[3 * tri + 1], q2 = b.tri_pool[3 * tri + 2];
+      const TriNode o = tri_node(t, make_float3(q0.x, q0.y, q0.z), make_float3(q1.x, q1.y, q1.z),
+                                 make_float3(q2.x, q2.y, q2.z), make_float3(q0.w, q1.w, q2.w));
+      const cf D = slot == 0 ? o.d.Da : (slot == 1 ? o.d.Db : o.d.Dc);
+      const float3 cs = o.c[slot];
+#pragma unroll
+      for (int r = 0; r < 3; ++r) {  // df/dv = -2 (c_s F + gamma k d D_s)
+        const float cr = comp(cs, r), gk = o.gam * k * comp(t.dh, r);
+        gr[r] += -2.0f * (cr * o.d.F.re + gk * D.re);
+        gi[r] += -2.0f * (cr * o.d.F.im + gk * D.im);
+      }
+    }
+    const int64_t row = vmap[v];
+#pragma unroll
+    for (int r = 0; r < 3; ++r) {
+      const cf val = cmul(cf{gr[r], gi[r]}, scl);
+      G[(row + r) * kg.Q + q] = make_float2(val.re, val.im);
+    }
+  }
+}
+
+}  // namespace
+
+int launch_jacobian(const pi_kgrid_impl* kg, const pi_batch_impl* b, float2* G, cudaStream_t s) {
+  std::vector<JacObj> tri, surf, mesh;
+  int64_t row = 0, vstart = 0;
+  for (int i = 0; i < b->n_obj; ++i) {
+    const HostObjInfo& in = b->info[i];
+    JacObj o{};
+    o.obj = i;
+    o.row0 = row;
+    o.src = static_cast<const unsigned char*>(b->d_src) + in.src_off;
+    o.dofs = b->d_dofs + in.dof_off;
+    if (in.dof_type == PI_DOF_TRIANGLE_MESH) {
+      o.kind = JAC_MESH_TRI;
+      o.vstart = vstart;
+      o.nverts = in.n_dofs / 3;
+      vstart += o.nverts;
+      mesh.push_back(o);
+    } else if (in.n_dofs != 12) {
+      return fail(PI_ERR_UNSUPPORTED, "the Jacobian supports AffineDoF (12) and TriangleMeshDoF objects");
+    } else if (in.geom_type == PI_GEOM_TRIANGLE) {
+      o.kind = JAC_AFFINE_TRI;
+      tri.push_back(o);
+    } else {
+      o.kind = JAC_AFFINE_SURF;
+      surf.push_back(o);
+    }
+    row += in.n_dofs;
+  }
+  if (!mesh.empty() && !b->d_vrow) return fail(PI_ERR_UNSUPPORTED, "vertex adjacency missing for TriangleMeshDoF objects");
+  const size_t nj = tri.size() + surf.size() + mesh.size();
+  if (nj == 0) return PI_OK;
+  if (nj > 65535) return fail(PI_ERR_UNSUPPORTED, "more than 65535 objects in one Jacobian");
+  std::vector<JacObj> all(tri);
+  all.insert(all.end(), surf.begin(), surf.end());
+  all.insert(all.end(), mesh.begin(), mesh.end());
+  JacObj* d = nullptr;
+  PI_CUDA(cudaMallocAsync((void**)&d, nj * sizeof(JacObj), s));
+  PI_CUDA(cudaMemcpyAsync(d, all.data(), nj * sizeof(JacObj), cudaMemcpyHostToDevice, s));
+  const KGridDev K = kg->dev;
+  const BatchDev B = b->dev();
+  const unsigned gx = (unsigned)(((int64_t)((K.M + 31) / 32) * K.L + JAC_WARPS - 1) / JAC_WARPS);
+  if (!tri.empty()) {
+    jac_affine_tri_kernel<<<dim3(gx, (unsigned)tri.size()), JAC_THREADS, 0, s>>>(K, B, d, G);
+    PI_LAUNCHED("jac_affine_tri_kernel");
+  }
+  if (!surf.empty()) {
+    jac_affine_surf_kernel<<<dim3(gx, (unsigned)surf.size()), JAC_THREADS, 0, s>>>(K, B, d + tri.size(), G);
+    PI_LAUNCHED("jac_affine_surf_kernel");
+  }
+  if (!mesh.empty()) {
+    jac_mesh_kernel<<<dim3(gx, (unsigned)mesh.size()), JAC_THREADS, 0, s>>>(K, B, d + tri.size() + surf.size(),
+                                                                             b->d_vrow, b->d_vent, b->d_vmap, G);
+    PI_LAUNCHED("jac_mesh_kernel");
+  }
+  PI_CUDA(cudaFreeAsync(d, s));
+  return PI_OK;
+}
+
+}  // namespace pi

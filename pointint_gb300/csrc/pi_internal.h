@@ -138,6 +138,9 @@ int launch_adjoint_elements(const pi_kgrid_impl* kg, const pi_batch_impl* b, con
 int launch_dof_gradients(const pi_kgrid_impl* kg, pi_batch_impl* b, const float2* Jw, const double* W_host,
                          double* grad, void* ws, size_t ws_bytes, cudaStream_t s);
 int launch_to_double2(const float2* J, int64_t n, double* out, cudaStream_t s);
+// G[d][q] = sqrt|w_q| dA(k_q)/dtheta_d for the concatenated DoF vector
+// (dof_gradient_size(b) rows of Q complex64), origin phase included.
+int launch_jacobian(const pi_kgrid_impl* kg, const pi_batch_impl* b, float2* G, cudaStream_t s);
 // Serving evaluations: grid (ff_serve_grid_x(kg), n_evals), ff_serve_threads().
 int ff_serve_grid_x(const pi_kgrid_impl* kg);
 int ff_serve_threads();
