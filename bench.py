@@ -421,7 +421,61 @@ def configs_bench(args, flush):
     out["surfels64"] = {"workload": meta4["workload"], "sample_objects": len(objs4), "forward_ms": ms_f,
                         "forward_disk_k_evals_per_s": evals4 / (ms_f / 1e3), "forward_backward_ms": ms_fb,
                         "backward_over_forward": (ms_fb - ms_f) / ms_f}
+    del scene
+    out["hessian256"], out["align"] = hessian_align_bench(flush)
     return out
+
+
+def hessian_align_bench(flush):
+    """Gauss-Newton Hessian of the 256-object matrix (DoF Jacobian of 3,072
+    rows + FP32 contraction) and the alignment caller (an icosphere-4
+    ellipsoid moving onto a box, N_k = 76,928): one similarity evaluation with gradient and
+    Hessian, and a full damped-Newton run from the warm start (host wall-clock,
+    results read back each evaluation)."""
+    import torch
+    from pointint_gb300 import align, configs, core, geometry as G
+    kg, objs, meta = configs.matrix256()
+    b = core.ObjectBatch(objs)
+    Gm = torch.empty((12 * len(objs), kg.num_nodes), dtype=torch.complex64, device="cuda")
+    ms_j = _timed(lambda: core.dof_jacobian(kg, b, out=Gm), flush, reps=2)
+    H = {}
+    ms_h = _timed(lambda: H.__setitem__("H", core.contract(kg, Gm, "fp32")), flush, reps=2)
+    hess = {"workload": meta["workload"] + "; Gauss-Newton Hessian over all 12 x 256 AffineDoFs",
+            "dofs": int(Gm.shape[0]), "jacobian_ms": ms_j, "contraction_ms": ms_h,
+            "jacobian_tri_k_evals_per_s": meta["n_triangles"] * kg.num_nodes / (ms_j / 1e3),
+            "contraction_tflops": 4.0 * kg.num_nodes * Gm.shape[0] ** 2 / (ms_h / 1e3) / 1e12}
+    del Gm, b, H
+    torch.cuda.empty_cache()
+    rng = np.random.default_rng(0)
+    V, F = G.icosphere(4)
+    g2 = G.make_triangle_mesh((V * np.array([1.4, 0.9, 0.6])) @ G.random_rotation(rng).T + 0.3, F)
+    Vb, Fb = G.box_mesh([1.6, 1.1, 0.8])
+    g1 = G.make_triangle_mesh(Vb @ G.random_rotation(rng).T, Fb)
+    with align.Aligner(g1, g2, kg) as a:
+        V1 = a.fixed_volume()
+        d0 = align.compute_warm_start(g1, g2)
+        a.similarity(d0, align.SIM_DICE, V1, align.SIM_ALL)
+        ts = []
+        for _ in range(5):
+            t0 = time.perf_counter()
+            a.similarity(d0, align.SIM_DICE, V1, align.SIM_ALL)
+            ts.append((time.perf_counter() - t0) * 1e3)
+        tf = []
+        for _ in range(5):
+            t0 = time.perf_counter()
+            a.similarity(d0, align.SIM_DICE, V1, align.SIM_FUNC_ONLY)
+            tf.append((time.perf_counter() - t0) * 1e3)
+        s0 = a.similarity(d0, align.SIM_DICE, V1, align.SIM_FUNC_ONLY).similarity
+        t0 = time.perf_counter()
+        st = a.optimize(d0, align.SIM_DICE, V1, 1e-6, 20, 0.1)
+        run_ms = (time.perf_counter() - t0) * 1e3
+    al = {"workload": "alignment, Dice: a moving icosphere-4 ellipsoid (5120 tris, axes 1.4/0.9/0.6) onto a "
+                      "fixed rotated box (12 tris), N_k = 76,928, from the moment warm start",
+          "similarity_grad_hess_ms": statistics.median(ts), "similarity_value_ms": statistics.median(tf),
+          "optimize_ms": run_ms, "newton_iterations": st.iteration + 1, "accepted_steps": st.steps,
+          "evaluations": st.evaluations, "similarity_start": s0, "similarity_end": st.similarity,
+          "status": st.status}
+    return hess, al
 
 
 def serving_bench(args, kg, objs, batch, contraction, flush):

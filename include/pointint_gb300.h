@@ -335,6 +335,61 @@ int pi_server_stats_get(pi_server s, pi_server_stats* st);
 /* Waits for the queries already admitted, fails the pending ones, frees everything. */
 int pi_server_destroy(pi_server s);
 
+/* ---- alignment caller: similarity measures, damped Newton, warm start ---------
+ * cpp/app/align (similarity_measure.hpp:10-48, optimizer.hpp:11-33,
+ * warm_start.hpp:9-34), headless.  Geometry 1 is fixed at the identity,
+ * geometry 2 moves under an AffineDoF (12 DoFs [t, A row-major]); the
+ * objective is -log(similarity). */
+enum { PI_SIM_OCHIAI = 0, PI_SIM_JACCARD = 1, PI_SIM_DICE = 2 };
+enum { PI_SIM_FUNC_ONLY = 1, PI_SIM_GRADIENT = 2, PI_SIM_HESSIAN = 4, PI_SIM_FUNC_GRAD = 3, PI_SIM_ALL = 7 };
+
+/* OptimizationState (optimizer.hpp:12-19) plus two counters. */
+typedef struct {
+  double dofs[12];
+  double similarity;       /* similarity at the last gradient evaluation */
+  double similarity_loss;  /* -log(similarity) there */
+  int32_t iteration;
+  int32_t converged;
+  int32_t steps;           /* accepted Newton steps */
+  int32_t evaluations;     /* similarity evaluations (gradient + line search) */
+  char status[64];
+} pi_optimization_state;
+
+typedef struct pi_aligner_s* pi_aligner;
+
+/* Holds the k-grid and both geometries on the device (host inputs; the DoF
+ * fields of geom1/geom2 are ignored), and evaluates geometry 1's form factors
+ * once. */
+int pi_aligner_create(const pi_object* geom1, const pi_object* geom2, const double* dirs, const double* kmag,
+                      const double* w, int64_t Q, pi_aligner* out);
+int pi_aligner_destroy(pi_aligner a);
+/* Fourier self-volume of geometry 1 on the aligner's grid: the V1 that the
+ * reference app passes in (compute_intersection_volume_cuda(geom1, geom1),
+ * cpp/app/align/main.cpp:224-230). */
+int pi_aligner_fixed_volume(pi_aligner a, double* V1);
+/* compute_similarity (similarity_measure.hpp:37-48): value = -log(max(s, 1e-10)),
+ * similarity = s; grad (12) and hess (12 x 12 row-major) of the value when the
+ * flags ask for them (else may be NULL).  The Hessian is the reference's
+ * Gauss-Newton form (zero Hessian of the intersection volume). */
+int pi_similarity(pi_aligner a, const double* dofs2, int measure, double V1, int flags, double* value,
+                  double* similarity, double* grad, double* hess);
+/* optimize_alignment (optimizer.hpp:22-33): Newton steps on the PSD projection
+ * of the Hessian plus damping I, Armijo backtracking (c = 0.1, factor 0.5, at
+ * most 20 halvings, alpha_min = 1e-10); stops when |grad| < tolerance.  Like the
+ * reference, a run that stops without converging reports "Reached max iterations". */
+int pi_optimize_alignment(pi_aligner a, const double* initial_dofs, int measure, double V1, double tolerance,
+                          int max_iterations, double damping, pi_optimization_state* state);
+/* compute_moments (warm_start.hpp:17-24) under the AffineDoF dofs (host
+ * geometry): volume, centroid (3), covariance (3 x 3 row-major).  No GPU. */
+int pi_compute_moments(const pi_object* geom, const double* dofs, double* volume, double* centroid,
+                       double* covariance);
+/* compute_warm_start (warm_start.hpp:26-34): the 12 AffineDoF parameters of
+ * the similarity transform matching geometry 2's moments to geometry 1's.
+ * Principal axes are taken with ascending eigenvalues and each axis's
+ * largest-magnitude component positive (the reference leaves these signs to
+ * its eigen-solver).  No GPU. */
+int pi_compute_warm_start(const pi_object* geom1, const pi_object* geom2, double* dofs_out);
+
 #ifdef __cplusplus
 }
 #endif

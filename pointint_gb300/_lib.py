@@ -59,6 +59,16 @@ class ServerStats(ctypes.Structure):
                [("tuned_items_per_sm", ctypes.c_int32 * 4)]
 
 
+class OptimizationState(ctypes.Structure):
+    """pi_optimization_state (the reference's OptimizationState plus two counters)."""
+    _fields_ = [("dofs", ctypes.c_double * 12), ("similarity", ctypes.c_double), ("similarity_loss", ctypes.c_double),
+                ("iteration", ctypes.c_int32), ("converged", ctypes.c_int32), ("steps", ctypes.c_int32),
+                ("evaluations", ctypes.c_int32), ("status", ctypes.c_char * 64)]
+
+
+SIM_OCHIAI, SIM_JACCARD, SIM_DICE = 0, 1, 2
+SIM_FUNC_ONLY, SIM_GRADIENT, SIM_HESSIAN, SIM_FUNC_GRAD, SIM_ALL = 1, 2, 4, 3, 7
+
 QUERY_PENDING, QUERY_RUNNING, QUERY_DONE, QUERY_FAILED, QUERY_CANCELLED = 0, 1, 2, 3, 4
 
 _lock = threading.Lock()
@@ -122,6 +132,13 @@ SIGNATURES = {
     "pi_server_release": (I32, [P, ctypes.c_uint64]),
     "pi_server_stats_get": (I32, [P, ctypes.POINTER(ServerStats)]),
     "pi_server_destroy": (I32, [P]),
+    "pi_aligner_create": (I32, [OBJP, OBJP, P, P, P, I64, PP]),
+    "pi_aligner_destroy": (I32, [P]),
+    "pi_aligner_fixed_volume": (I32, [P, ctypes.POINTER(D)]),
+    "pi_similarity": (I32, [P, P, I32, D, I32, ctypes.POINTER(D), ctypes.POINTER(D), P, P]),
+    "pi_optimize_alignment": (I32, [P, P, I32, D, D, I32, D, ctypes.POINTER(OptimizationState)]),
+    "pi_compute_moments": (I32, [OBJP, P, ctypes.POINTER(D), P, P]),
+    "pi_compute_warm_start": (I32, [OBJP, OBJP, P]),
 }
 
 

@@ -21,7 +21,7 @@ LIB = os.path.join(HERE, "libpointint_gb300.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = ["host.cpp", "capi.cu", "formfactor.cu", "contract.cu", "contract_tc.cu", "contract_group.cu", "adjoint.cu",
-           "jacobian.cu",
+           "jacobian.cu", "align.cpp",
            "server.cpp"]
 
 
