@@ -15,8 +15,8 @@
 // sum kept in tensor memory (round-to-nearest adds), and a work item can then
 // cover a long k range with one partial tile.
 //
-// Persistent CTA (one per SM) of 15 warps:
-//   warps 8-9   loaders.  Rows contiguous in memory (one volume matrix over a
+// Persistent CTA (one per SM) of 23 warps:
+//   warps 16-17 loaders.  Rows contiguous in memory (one volume matrix over a
 //               caller's J): one lane issues 2D TMA boxes of 128 rows x 32
 //               FP32 values, two per tile and chunk.  Rows gathered from
 //               anywhere (the serving pool): 16-byte cp.async copies, one
@@ -25,17 +25,17 @@
 //               the TMA (16-byte unit u of row r at r * 128 + ((u ^ r % 8) * 16)
 //               within each 16 KB half-box), which keeps the converters'
 //               reads free of bank conflicts;
-//   warps 0-7   converters: each thread takes 16 complex values of one row of
+//   warps 0-15  converters: each thread takes 8 complex values of one row of
 //               each tile, applies the translation phase (direction-major rows:
-//               the direction is fixed over the 16 values, so d.c is formed
+//               the direction is fixed over the 8 values, so d.c is formed
 //               once in double-float and each value needs one product with
 //               kmag / 2 pi and a quarter-turn reduction), splits hi/lo and
 //               writes both halves back in place as 128-byte-swizzled K-major
 //               UMMA operands;
-//   warp 10     MMA issuer (one lane) and tensor-memory owner: columns 0-255
+//   warp 18     MMA issuer (one lane) and tensor-memory owner: columns 0-255
 //               hold two chain accumulators (double-buffered), 256-383 the
 //               running sum;
-//   warps 11-14 epilogue: chain -> running sum; at the end of an item the sum
+//   warps 19-22 epilogue: chain -> running sum; at the end of an item the sum
 //               goes to the item's FP32 partial tile.
 // Every wait is bounded (~2 s of SM clock); on expiry the kernel records an
 // error code, every role leaves its loop, in-flight copies and MMAs are
@@ -65,7 +65,9 @@ constexpr int BOXB = 2 * HALF;                   // 32 KB: one tile's FP32 chunk
 constexpr int STAGE = 2 * BOXB;                  // 64 KB: two tiles = four operand blocks
 constexpr int NST = 3;
 constexpr int SMEM = NST * STAGE + 1024;         // + alignment slack
-constexpr int CWARPS = 8, LWARP0 = 8, MWARP = 10, EWARP0 = 11, NWARPS = 15;
+constexpr int CWARPS = 16, LWARP0 = 16, MWARP = 18, EWARP0 = 19, NWARPS = 23;
+constexpr int CV = 8;                            // complex values of one row per converter thread and tile
+static_assert(CWARPS * 32 * CV == GM * CK, "converters cover a tile's chunk exactly once");
 static_assert(LWARP0 + 2 == MWARP && MWARP + 1 == EWARP0 && EWARP0 + 4 == NWARPS, "warp roles");
 constexpr int NTHREADS = NWARPS * 32;
 constexpr int TMEM_COLS = 512;
@@ -84,20 +86,16 @@ template <int OP> constexpr uint32_t op_idesc() { return idesc(OP == GROUP_OP_F1
 
 enum { ERR_LOAD = 1, ERR_CONVERT = 2, ERR_MMA = 3, ERR_EPILOGUE = 4, ERR_CAPACITY = 5 };
 
-// x[0..31] = 16 complex values of one row, columns col0 .. col0 + 15 of a
-// direction-major row (col = j L + r).  Multiplies them by e^{2 pi i kturn_r (d_j . c)}.
-// sd: the chunk's staged directions (hi, lo of the chunk's first direction,
-// then of the next one), j0 the chunk's first direction.
-__device__ __forceinline__ void apply_phase(float* x, int64_t col0, float3 ch, float3 cl, const GroupDev& g,
-                                            const float2* kt, const float4* sd, int64_t j0) {
-  const int64_t j = col0 / g.L;
-  if (j >= g.M) return;  // padding columns hold zeros
-  const int r0 = (int)(col0 - j * g.L);
-  const int slot = j == j0 ? 0 : 2;
-  const float4 h = sd[slot], l = sd[slot + 1];
+// x[0..2 NV - 1] = NV complex values of one row of a direction-major row
+// (col = j L + r), at radii r0 .. r0 + NV - 1 of one direction (L is a
+// multiple of 16).  Multiplies them by e^{2 pi i kturn_r (d_j . c)}.
+// d: the direction's staged hi, lo pair.
+template <int NV>
+__device__ __forceinline__ void apply_phase(float* x, int r0, float3 ch, float3 cl, const float2* kt, const float4* d) {
+  const float4 h = d[0], l = d[1];
   const df s = cdot2(make_float3(h.x, h.y, h.z), make_float3(l.x, l.y, l.z), ch, cl);
 #pragma unroll
-  for (int i = 0; i < 16; ++i) {
+  for (int i = 0; i < NV; ++i) {
     const float2 k = kt[r0 + i];
     // turns = kturn * s: the integer part of the leading product is removed
     // exactly; the rounding error of that product and the small cross terms
@@ -117,14 +115,15 @@ __device__ __forceinline__ void apply_phase(float* x, int64_t col0, float3 ch, f
   }
 }
 
-// Split 32 FP32 values (this thread's half of a 64-value K row), times the
-// row scale, into 16-bit hi and lo and store both, 128-byte swizzled: K chunk
-// (16 B) u of row r lives at (r / 8) * 1024 + (r % 8) * 128 + ((u ^ (r % 8)) * 16).
-template <int OP>
-__device__ __forceinline__ void store_split(uint8_t* op, int row, int h, const float* x, float scale) {
+// Split 8 NU FP32 values (part q of a 64-value K row), times the row scale,
+// into 16-bit hi and lo and store both, 128-byte swizzled: K chunk (16 B) u of
+// row r lives at (r / 8) * 1024 + (r % 8) * 128 + ((u ^ (r % 8)) * 16), and
+// part q covers units NU q .. NU q + NU - 1.
+template <int OP, int NU>
+__device__ __forceinline__ void store_split(uint8_t* op, int row, int q, const float* x, float scale) {
   const uint32_t rb = (uint32_t)((row >> 3) * 1024 + (row & 7) * 128);
 #pragma unroll
-  for (int p = 0; p < 4; ++p) {
+  for (int p = 0; p < NU; ++p) {
     uint32_t hi[4], lo[4];
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
@@ -132,7 +131,7 @@ __device__ __forceinline__ void store_split(uint8_t* op, int row, int h, const f
       if (OP == GROUP_OP_F16) split2_f16(a * scale, b * scale, &hi[i], &lo[i]);
       else split2_bf16(a, b, &hi[i], &lo[i]);
     }
-    const uint32_t off = rb + ((uint32_t)((4 * h + p) ^ (row & 7)) << 4);
+    const uint32_t off = rb + ((uint32_t)((NU * q + p) ^ (row & 7)) << 4);
     *reinterpret_cast<uint4*>(op + off) = make_uint4(hi[0], hi[1], hi[2], hi[3]);
     *reinterpret_cast<uint4*>(op + OPB + off) = make_uint4(lo[0], lo[1], lo[2], lo[3]);
   }
@@ -289,7 +288,12 @@ group_split3_kernel(const GroupDev g, const __grid_constant__ CUtensorMap xmap) 
     }
   } else if (warp < CWARPS) {
     // ---------------- converters ----------------
-    const int row = warp * 16 + (lane & 15), h = lane >> 4;
+    // thread (row, q): 8 complex values (quarter q of the chunk's 32 columns)
+    // of one row of each tile; a warp owns all four quarters of 8 rows.  The
+    // hi and lo operand rows of row r occupy exactly the bytes of row r's
+    // FP32 input (first and second half-box), so a warp overwrites only
+    // inputs it has read itself and needs no barrier with the other warps.
+    const int row = warp * 8 + (lane >> 2), q = lane & 3;
     int64_t gc = 0;
     bool ok = true;
     for (int it = blockIdx.x; it < n_items && ok; it += gridDim.x) {
@@ -312,42 +316,49 @@ group_split3_kernel(const GroupDev g, const __grid_constant__ CUtensorMap xmap) 
         const int s = (int)(gc % NST);
         const int64_t rnd = gc / NST;
         ok = mbar_wait(smem_u32(&load_bar[s]), (uint32_t)(rnd & 1), err, ERR_CONVERT);
+        ok = __all_sync(0xffffffffu, ok);
+        if (!ok) break;
         uint8_t* st = smem + s * STAGE;
-        float xa[32], xb[32];
-        if (ok) {
-          if (va) {
+        const int64_t col0 = ((int64_t)w.chunk0 + (int64_t)c * w.cstride) * CK + CV * q;
+        const int64_t nvalid = g.ncols - col0;  // < CV only in the last chunk of a ragged row
+        // Direction and first radius of this thread's values: the chunk starts
+        // at radius rc of direction jc, and with L a multiple of 16 the
+        // thread's 8 values sit in direction jc or jc + 1 (32-bit arithmetic:
+        // phase launches have rows of fewer than 2^31 columns).
+        bool phase_ok = false;
+        int r0 = 0, dslot = 0;
+        if (PHASE) {
+          const uint32_t cbase = (uint32_t)(((int64_t)w.chunk0 + (int64_t)c * w.cstride) * CK);
+          const uint32_t jc = cbase / (uint32_t)g.L;
+          r0 = (int)(cbase - jc * (uint32_t)g.L) + CV * q;
+          uint32_t j = jc;
+          if (r0 >= g.L) { r0 -= g.L; ++j; dslot = 2; }
+          phase_ok = j < (uint32_t)g.M;  // padding columns past the last direction hold zeros
+        }
+        // One tile at a time (fewer live registers).  Every lane of the warp
+        // has read a tile's inputs before any of its outputs overwrites them.
 #pragma unroll
-            for (int m = 0; m < 8; ++m) {
-              const float4 v = *reinterpret_cast<const float4*>(st + stage_off(row, 8 * h + m));
-              xa[4 * m] = v.x; xa[4 * m + 1] = v.y; xa[4 * m + 2] = v.z; xa[4 * m + 3] = v.w;
+        for (int t = 0; t < 2; ++t) {
+          const bool v = t == 0 ? va : vb;
+          float x[2 * CV];
+          if (v) {
+#pragma unroll
+            for (int m = 0; m < CV / 2; ++m) {
+              const float4 u = *reinterpret_cast<const float4*>(st + t * BOXB + stage_off(row, (CV / 2) * q + m));
+              x[4 * m] = u.x; x[4 * m + 1] = u.y; x[4 * m + 2] = u.z; x[4 * m + 3] = u.w;
             }
           }
-          if (vb) {
+          __syncwarp();
+          if (v) {
+            if (nvalid < CV) {
 #pragma unroll
-            for (int m = 0; m < 8; ++m) {
-              const float4 v = *reinterpret_cast<const float4*>(st + BOXB + stage_off(row, 8 * h + m));
-              xb[4 * m] = v.x; xb[4 * m + 1] = v.y; xb[4 * m + 2] = v.z; xb[4 * m + 3] = v.w;
+              for (int i = 0; i < CV; ++i)
+                if (i >= nvalid) x[2 * i] = x[2 * i + 1] = 0.f;
             }
+            if (PHASE && phase_ok)
+              apply_phase<CV>(x, r0, t == 0 ? cah : cbh, t == 0 ? cal : cbl, kt, &sdir[PHASE ? s : 0][dslot]);
+            store_split<OP, CV / 4>(st + t * 2 * OPB, row, q, x, t == 0 ? sa : sb);
           }
-        }
-        // Every converter has read its inputs before any output overwrites
-        // the staging boxes; all converters leave together on an error.
-        if (bar_any(1, CWARPS * 32, !ok)) { ok = false; break; }
-        const int64_t col0 = ((int64_t)w.chunk0 + (int64_t)c * w.cstride) * CK + 16 * h;
-        const int64_t nvalid = g.ncols - col0;  // < 16 only in the last chunk of a ragged row
-        if (nvalid < 16) {
-#pragma unroll
-          for (int i = 0; i < 16; ++i)
-            if (i >= nvalid) { xa[2 * i] = xa[2 * i + 1] = 0.f; xb[2 * i] = xb[2 * i + 1] = 0.f; }
-        }
-        const int64_t j0 = (((int64_t)w.chunk0 + (int64_t)c * w.cstride) * CK) / (PHASE ? g.L : 1);
-        if (va) {
-          if (PHASE) apply_phase(xa, col0, cah, cal, g, kt, sdir[PHASE ? s : 0], j0);
-          store_split<OP>(st, row, h, xa, sa);
-        }
-        if (vb) {
-          if (PHASE) apply_phase(xb, col0, cbh, cbl, g, kt, sdir[PHASE ? s : 0], j0);
-          store_split<OP>(st + 2 * OPB, row, h, xb, sb);
         }
         fence_proxy_async();
         __syncwarp();
@@ -407,7 +418,7 @@ group_split3_kernel(const GroupDev g, const __grid_constant__ CUtensorMap xmap) 
     for (int it = blockIdx.x; it < n_items && ok; it += gridDim.x) {
       const GItem w = group_item(g, it);
       const int nch = (w.nchunks + CHAIN - 1) / CHAIN;
-      const int ncb = (w.nb + 31) >> 5;
+      const int ncb = (w.nb + 15) >> 4;
       float* out = g.partials + (int64_t)it * (GM * GM) + (int64_t)row * GM;
       for (int ch = 0; ch < nch; ++ch, ++gch) {
         const int b = (int)(gch & 1);
@@ -415,22 +426,22 @@ group_split3_kernel(const GroupDev g, const __grid_constant__ CUtensorMap xmap) 
         fence_after();
         const bool first = ch == 0, last = ch == nch - 1;
 #pragma unroll 1
-        for (int cb = 0; cb < 4; ++cb) {
+        for (int cb = 0; cb < 8; ++cb) {
           if (cb >= ncb) break;  // warp-uniform
-          float v[32];
-          tmem_ld32(tl + (uint32_t)(b * GM + cb * 32), v);
+          float v[16];
+          tmem_ld16(tl + (uint32_t)(b * GM + cb * 16), v);
           if (!first) {
-            float r[32];
-            tmem_ld32(tl + SUM_COL + (uint32_t)(cb * 32), r);
+            float r[16];
+            tmem_ld16(tl + SUM_COL + (uint32_t)(cb * 16), r);
 #pragma unroll
-            for (int i = 0; i < 32; ++i) v[i] += r[i];
+            for (int i = 0; i < 16; ++i) v[i] += r[i];
           }
           if (!last) {
-            tmem_st32(tl + SUM_COL + (uint32_t)(cb * 32), v);
+            tmem_st16(tl + SUM_COL + (uint32_t)(cb * 16), v);
           } else if (row < w.na) {
 #pragma unroll
-            for (int i = 0; i < 32; i += 4)
-              *reinterpret_cast<float4*>(out + cb * 32 + i) = make_float4(v[i], v[i + 1], v[i + 2], v[i + 3]);
+            for (int i = 0; i < 16; i += 4)
+              *reinterpret_cast<float4*>(out + cb * 16 + i) = make_float4(v[i], v[i + 1], v[i + 2], v[i + 3]);
           }
         }
         fence_before();
@@ -598,6 +609,8 @@ int launch_group_contract(const GroupDev& g, const CUtensorMap* xmap, bool all_t
   if (rc) return rc;
   if (g.phase && (g.L <= 0 || g.L > GROUP_MAX_L || g.L % 16 != 0))
     return fail(PI_ERR_UNSUPPORTED, "translation phases need 16 | L <= 512 radial nodes per direction");
+  if (g.phase && g.ncols >= (int64_t(1) << 31))
+    return fail(PI_ERR_UNSUPPORTED, "translation phases support rows of fewer than 2^31 columns");
   if ((all_tma || g.tile_tma) && !xmap) return fail(PI_ERR_INVALID_ARGUMENT, "TMA loads need a tensor map");
   CUtensorMap none;
   std::memset(&none, 0, sizeof(none));

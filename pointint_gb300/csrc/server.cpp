@@ -789,6 +789,7 @@ int pi_server_create(pi_kgrid kg, const pi_object* library, int n_library, const
     return fail(PI_ERR_UNSUPPORTED,
                 "the serving path needs a Gauss-Legendre x Lebedev k-grid with a multiple of 16 radial nodes (<= 512)");
   if (!kg->all_positive) return fail(PI_ERR_UNSUPPORTED, "the serving path needs non-negative quadrature weights");
+  if (kg->Q >= (int64_t(1) << 31) - 64) return fail(PI_ERR_UNSUPPORTED, "the serving path supports fewer than 2^31 k-nodes");
   pi_server_config c{};
   if (cfg_in) c = *cfg_in;
   if (c.max_batch_queries <= 0) c.max_batch_queries = 64;
