@@ -90,13 +90,6 @@ __device__ __forceinline__ df cdot2(float3 dh, float3 dl, float3 xh, float3 xl) 
 
 struct cf { float re, im; };
 
-// e^{i x} for a double-float phase x (|x| < ~1e5): Cody-Waite reduction by
-// pi/2 to r in [-pi/4, pi/4] (fmaf(-n, A, x) is exact: the result needs at
-// most 23 significant bits), then this project's own least-squares
-// polynomials for sin(r)/r (degree 4 in r^2) and cos(r) (degree 5 in r^2),
-// fitted on Chebyshev-spaced samples of [-pi/4, pi/4]; FP32 evaluation error
-// <= 7e-8 each, about 5x below the hardware sin/cos approximation.  The
-// quadrant n mod 4 rotates the result.
 // e^{i (r + q pi/2)} for r in [-pi/4, pi/4]: this project's own least-squares
 // polynomials for sin(r)/r (degree 4 in r^2) and cos(r) (degree 5 in r^2),
 // fitted on Chebyshev-spaced samples of [-pi/4, pi/4]; FP32 evaluation error
