@@ -56,6 +56,9 @@ def parse():
     p.add_argument("--serve-burst", type=int, default=200, help="256-object scene queries in the warm burst")
     p.add_argument("--objects", type=int, default=256,
                    help="object count of the matrix workload (256 = the benchmark; smaller only for profiling)")
+    p.add_argument("--profile-case", default=None,
+                   choices=["contract", "adjoint", "surfel_adjoint", "jacobian", "serve"],
+                   help="run one kernel family's workload a few times (for ncu captures) instead of the benchmark")
     return p.parse_args()
 
 
@@ -629,8 +632,74 @@ def e2e_host(kg, objs, precision, steps, evals_step, world):
             "ms_per_step": dt * 1e3, "entry_point": "pi_volume_matrix_host"}
 
 
+def profile_case(name: str):
+    """One kernel family's workload, three times (the first launch warms up),
+    with CUDA-event times printed as one JSON line.  For ncu captures of the
+    kernels that the benchmark line does not time on their own:
+      contract        FP32 / TF32x3 / BF16x3 / FP16x3 contractions of the 256-object J
+      adjoint         dV/dtheta of the 256-object matrix (W = 1): adj_tri_kernel + chain
+      surfel_adjoint  per-disk position / normal gradients, 8 objects x 50,000 disks
+      jacobian        DoF Jacobian of the 256-object matrix (3,072 rows)
+      serve           the 256-object scene re-queried under translations (20 queries)"""
+    import torch
+    from pointint_gb300 import configs, core
+    out = {"case": name}
+
+    def timed(fn, reps=3):
+        ts = []
+        for _ in range(reps):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record()
+            fn()
+            b.record()
+            b.synchronize()
+            ts.append(a.elapsed_time(b))
+        return ts
+
+    if name in ("contract", "adjoint", "jacobian", "serve"):
+        kg, objs, meta = configs.matrix256()
+        batch = core.ObjectBatch(objs)
+        J = core.form_factors(kg, batch, True)
+        n = len(objs)
+        if name == "contract":
+            for p in ("fp32", "tf32x3", "bf16x3", "fp16x3"):
+                out[p + "_ms"] = timed(lambda: core.contract(kg, J, p))
+        elif name == "adjoint":
+            W = np.ones((n, n))
+            out["ms"] = timed(lambda: core.dof_gradients(kg, batch, J, W))
+        elif name == "jacobian":
+            G = torch.empty((12 * n, kg.num_nodes), dtype=torch.complex64, device="cuda")
+            out["ms"] = timed(lambda: core.dof_jacobian(kg, batch, out=G))
+        else:
+            from pointint_gb300.serving import Server
+            del J
+            rng = np.random.default_rng(0)
+            ids = np.arange(n, dtype=np.int32)
+            with Server(kg, objs, precision="fp16x3", autotune=False) as srv:
+                srv.query(ids, None, np.zeros((n, 3)))
+                t0 = time.perf_counter()
+                for _ in range(20):
+                    srv.query(ids, None, rng.normal(0.0, 0.5, size=(n, 3)))
+                out["ms_per_query"] = (time.perf_counter() - t0) * 1e3 / 20
+    else:
+        kg, objs, meta = configs.surfels64(n_objects=8)
+        scene = core.Scene(kg, objs)
+        c0, n0 = scene.surfel_params()
+
+        def fwd_bwd():
+            c = c0.clone().requires_grad_(True)
+            nn = n0.clone().requires_grad_(True)
+            scene.volume_matrix_of_surfels(c, nn).sum().backward()
+        out["ms"] = timed(fwd_bwd)
+    out["workload"] = meta["workload"]
+    print(json.dumps(out))
+
+
 def main():
     args = parse()
+    if args.profile_case:
+        profile_case(args.profile_case)
+        return
     if args.impl == "reference":
         run_reference(args)
     else:

@@ -260,7 +260,7 @@ adj_tri_kernel(KGridDev kg, BatchDev b, const AdjWork* __restrict__ work, const 
         const float al = k.hi * d1.hi, be = k.hi * d2.hi;
         TriDer d;
         if (k.hi * sp < 2.0f) d = tri_series_der(cis(df_mul_un(k, sm)), al, be);
-        else d = tri_generic_der(cis(df_mul_un(k, sa)), cis(df_mul_un(k, sb)), cis(df_mul_un(k, sc)), al, be);
+        else d = tri_generic_der_at(k, sa, sb, sc, al, be);
         // Re(conj(B) X) = B.re X.re + B.im X.im
         t0 = fmaf(Bv.x, d.F.re, fmaf(Bv.y, d.F.im, t0));
         ta = fmaf(k.hi, fmaf(Bv.x, d.Da.re, Bv.y * d.Da.im), ta);

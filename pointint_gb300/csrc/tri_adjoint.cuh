@@ -107,4 +107,12 @@ __device__ __forceinline__ TriDer tri_generic_der(cf Pa, cf Pb, cf Pc, float al,
   return d;
 }
 
+// The large-spread derivatives from the vertex phases, as an out-of-line call:
+// a kernel whose hot radius loop inlines this rarely taken path as well as the
+// series outgrows the instruction cache (the loop then stalls on instruction
+// fetch), while the call costs little on the few nodes that take it.
+static __device__ __noinline__ TriDer tri_generic_der_at(df k, df sa, df sb, df sc, float al, float be) {
+  return tri_generic_der(cis(df_mul_un(k, sa)), cis(df_mul_un(k, sb)), cis(df_mul_un(k, sc)), al, be);
+}
+
 }  // namespace pi
