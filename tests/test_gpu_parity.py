@@ -157,6 +157,29 @@ def test_single_k_compute_Ak(cuda, orc):
         assert abs(a - exact) <= 2e-6 * max(1.0, np.linalg.norm(k))
 
 
+def test_ball_transform(cuda, orc):
+    """Second analytic oracle: icospheres rescaled to the unit ball's volume
+    against the exact ball transform A(k) = i|k| F_ball(k)
+    (form_factor_helpers.cpp:162-173), |k| < 8.  The polyhedron differs from
+    the ball by O(h^2): the error falls ~4x per subdivision level and is
+    within 3e-5 of the ball's volume at level 5."""
+    kg = standard_kgrid(9, 16)
+    sel = kg.kmag < 8.0
+    sub = KGrid(kg.dirs[sel], kg.kmag[sel], kg.w[sel])
+    ex = np.array([1j * k * orc.exact_sphere_form_factor(k, 1.0) for k in sub.kmag])
+    vball = 4.0 / 3.0 * np.pi
+    errs = []
+    for level in (4, 5):
+        V, F = G.icosphere(level)
+        g = G.make_triangle_mesh(V, F)
+        s = (vball / G.self_volume(G.SceneObject(g))) ** (1.0 / 3.0)
+        obj = G.SceneObject(G.make_triangle_mesh(V * s, F))
+        A = core.form_factors(sub, core.ObjectBatch([obj]), False).cpu().numpy()[0]
+        errs.append(np.abs(A - ex).max() / vball)
+    print(f"\nball transform: max |A - exact| / V = {errs[0]:.2e} (level 4), {errs[1]:.2e} (level 5)")
+    assert errs[1] <= 3e-5 and errs[0] / errs[1] > 3.0
+
+
 def test_edge_cases(cuda, orc):
     """Empty object, degenerate triangle, k = 0 node, non-tensor grid with an
     odd node count, negative weights, object count not a multiple of 64."""
