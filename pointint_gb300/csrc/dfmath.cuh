@@ -131,24 +131,6 @@ __device__ __forceinline__ cf cmul(cf a, cf b) { return {a.re * b.re - a.im * b.
 __device__ __forceinline__ cf csub(cf a, cf b) { return {a.re - b.re, a.im - b.im}; }
 __device__ __forceinline__ cf cscale(cf a, float s) { return {a.re * s, a.im * s}; }
 
-// First divided difference of f(z) = e^{iz} at two points u, v = u + g, given
-// Pu = e^{iu}, Pv = e^{iv}.  Uses (Pv - Pu)/g for |g| >= 1/2 and otherwise the
-// cancellation-free form i e^{i(u+v)/2} sinc(g/2) with short Taylor series of
-// cos, sin and sinc on |g/2| < 1/4 (truncation < 1e-9).
-__device__ __forceinline__ cf dd1(cf Pu, cf Pv, float g) {
-  if (fabsf(g) >= 0.5f) {
-    float ig = __frcp_rn(g);
-    return cscale(csub(Pv, Pu), ig);
-  }
-  float x = 0.5f * g, x2 = x * x;
-  float c = fmaf(x2, fmaf(x2, fmaf(x2, -1.0f / 720.0f, 1.0f / 24.0f), -0.5f), 1.0f);
-  float sc = fmaf(x2, fmaf(x2, fmaf(x2, -1.0f / 5040.0f, 1.0f / 120.0f), -1.0f / 6.0f), 1.0f);  // sinc x
-  float s = x * sc;
-  // i * (c + i s) * sc = (-s sc) + i (c sc)
-  cf m = cmul(Pu, cf{c, s});
-  return {-m.im * sc, m.re * sc};
-}
-
 // Exact-ish division of a double-float by 3 (the FP32 quotient's remainder is
 // formed exactly with an FMA).
 __device__ __forceinline__ df df_div3(df a) {
@@ -238,27 +220,43 @@ __device__ __forceinline__ cf tri_series_eval(const TriPoly& t, float k) {
   return {re, im};
 }
 
+// First divided difference of f(z) = e^{iz} at two points u, v = u + g, given
+// Pu = e^{iu}, Pv = e^{iv}: (Pv - Pu)/g for |g| >= 1/2, otherwise the
+// cancellation-free form i e^{i(u+v)/2} sinc(g/2) with short Taylor series of
+// cos, sin and sinc on |g/2| < 1/4 (truncation < 1e-9).  Both forms are
+// evaluated and one is selected, so the lanes of a warp never split on |g|.
+__device__ __forceinline__ cf dd1(cf Pu, cf Pv, float g) {
+  const float ig = __frcp_rn(g);  // inf for g = 0, where the series form is taken
+  const cf big = cscale(csub(Pv, Pu), ig);
+  const float x = 0.5f * g, x2 = x * x;
+  const float c = fmaf(x2, fmaf(x2, fmaf(x2, -1.0f / 720.0f, 1.0f / 24.0f), -0.5f), 1.0f);
+  const float sc = fmaf(x2, fmaf(x2, fmaf(x2, -1.0f / 5040.0f, 1.0f / 120.0f), -1.0f / 6.0f), 1.0f);
+  const cf m = cmul(Pu, cf{c, x * sc});
+  const bool b = fabsf(g) >= 0.5f;
+  return {b ? big.re : -m.im * sc, b ? big.im : m.re * sc};
+}
+
 // tri_generic: spread D >= 2.  (f[R,Q] - f[P,R]) / (Q - P) with (P, Q) the pair
 // of vertices with the largest gap (|Q-P| = D, so the subtraction loses at
 // most a factor ~1/D of FP32 precision) and stable first differences.
 // Returns e[pa, pb, pc] given the vertex phasors and al = pb-pa, be = pc-pa.
+// The roles (P, Q, R) are chosen by selects, not a three-way branch: the lanes
+// of a warp hold different directions and pick different pairs, and a branch
+// would run all three cases for the warp.
 __device__ __forceinline__ cf tri_generic(cf Pa, cf Pb, cf Pc, float al, float be) {
   const float gab = al, gac = be, gbc = be - al;
-  cf fRQ, fPR;
-  float den;
-  if (fabsf(gab) >= fabsf(gac) && fabsf(gab) >= fabsf(gbc)) {  // P = a, Q = b, R = c
-    fRQ = dd1(Pc, Pb, -gbc);
-    fPR = dd1(Pa, Pc, gac);
-    den = gab;
-  } else if (fabsf(gac) >= fabsf(gbc)) {  // P = a, Q = c, R = b
-    fRQ = dd1(Pb, Pc, gbc);
-    fPR = dd1(Pa, Pb, gab);
-    den = gac;
-  } else {  // P = b, Q = c, R = a
-    fRQ = dd1(Pa, Pc, gac);
-    fPR = dd1(Pb, Pa, -gab);
-    den = gbc;
-  }
+  const float aab = fabsf(gab), aac = fabsf(gac), abc = fabsf(gbc);
+  const bool c1 = aab >= aac && aab >= abc;  // P = a, Q = b, R = c
+  const bool c2 = !c1 && aac >= abc;         // P = a, Q = c, R = b; else P = b, Q = c, R = a
+  // f[R, Q] = dd1(u1, v1, g1), f[P, R] = dd1(u2, v2, g2)
+  const cf u1 = c1 ? Pc : (c2 ? Pb : Pa);
+  const cf v1 = c1 ? Pb : Pc;
+  const float g1 = c1 ? -gbc : (c2 ? gbc : gac);
+  const cf u2 = c1 || c2 ? Pa : Pb;
+  const cf v2 = c1 ? Pc : (c2 ? Pb : Pa);
+  const float g2 = c1 ? gac : (c2 ? gab : -gab);
+  const float den = c1 ? gab : (c2 ? gac : gbc);
+  const cf fRQ = dd1(u1, v1, g1), fPR = dd1(u2, v2, g2);
   const float s = __frcp_rn(den);
   return {(fRQ.re - fPR.re) * s, (fRQ.im - fPR.im) * s};
 }

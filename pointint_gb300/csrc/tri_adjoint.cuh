@@ -65,45 +65,50 @@ __device__ __forceinline__ TriDer tri_series_der(cf P, float al, float be) {
   return d;
 }
 
-// G(h) = (e^{ih} - 1 - ih)/h^2 given E = e^{ih}.
+// G(h) = (e^{ih} - 1 - ih)/h^2 given E = e^{ih}: the direct form for
+// |h| >= 1/2, otherwise the series sum_m i^{m+2} h^m/(m+2)!, m = 0..9:
+//   Re = -1/2 + h^2/24 - h^4/720 + h^6/40320 - h^8/3628800
+//   Im = h (-1/6 + h^2/120 - h^4/5040 + h^6/362880 - h^8/39916800)
+// Both are evaluated and one is selected (no divergent branch).
 __device__ __forceinline__ cf Gfun(cf E, float h) {
-  if (fabsf(h) >= 0.5f) {
-    const float ih2 = __frcp_rn(h * h);
-    return {(E.re - 1.0f) * ih2, (E.im - h) * ih2};
-  }
-  // sum_m i^{m+2} h^m/(m+2)!, m = 0..9:
-  //   Re = -1/2 + h^2/24 - h^4/720 + h^6/40320 - h^8/3628800
-  //   Im = h (-1/6 + h^2/120 - h^4/5040 + h^6/362880 - h^8/39916800)
   const float h2 = h * h;
+  const float ih2 = __frcp_rn(h2);  // inf for h = 0, where the series is taken
   const float re = fmaf(h2, fmaf(h2, fmaf(h2, fmaf(h2, -1.0f / 3628800.0f, 1.0f / 40320.0f), -1.0f / 720.0f),
                                  1.0f / 24.0f), -0.5f);
   const float im = h * fmaf(h2, fmaf(h2, fmaf(h2, fmaf(h2, -1.0f / 39916800.0f, 1.0f / 362880.0f), -1.0f / 5040.0f),
                                      1.0f / 120.0f), -1.0f / 6.0f);
-  return {re, im};
+  const bool big = fabsf(h) >= 0.5f;
+  return {big ? (E.re - 1.0f) * ih2 : re, big ? (E.im - h) * ih2 : im};
 }
 
 __device__ __forceinline__ cf conjmul(cf a, cf b) { return {a.re * b.re + a.im * b.im, a.im * b.re - a.re * b.im}; }  // a conj(b)
 
+__device__ __forceinline__ cf csel(bool c, cf a, cf b) { return {c ? a.re : b.re, c ? a.im : b.im}; }
+
+// The roles (P, Q, R) are chosen by selects as in tri_generic, so lanes of a
+// warp that pick different pairs do not split.
 __device__ __forceinline__ TriDer tri_generic_der(cf Pa, cf Pb, cf Pc, float al, float be) {
   TriDer d;
   d.F = tri_generic(Pa, Pb, Pc, al, be);
   const float gab = al, gac = be, gbc = be - al;
+  const float aab = fabsf(gab), aac = fabsf(gac), abc = fabsf(gbc);
+  const bool c1 = aab >= aac && aab >= abc;  // P = a, Q = b, R = c
+  const bool c2 = !c1 && aac >= abc;         // P = a, Q = c, R = b; else P = b, Q = c, R = a
   // vertices as (phasor, relative phase): a = 0, b = al, c = be
-  int P, Q, R;
-  if (fabsf(gab) >= fabsf(gac) && fabsf(gab) >= fabsf(gbc)) { P = 0; Q = 1; R = 2; }
-  else if (fabsf(gac) >= fabsf(gbc)) { P = 0; Q = 2; R = 1; }
-  else { P = 1; Q = 2; R = 0; }
-  const cf ph[3] = {Pa, Pb, Pc};
-  const float z[3] = {0.f, al, be};
-  const float iden = __frcp_rn(z[Q] - z[P]);
+  const cf phP = csel(c1 || c2, Pa, Pb), phQ = csel(c1, Pb, Pc), phR = csel(c1, Pc, csel(c2, Pb, Pa));
+  const float zP = c1 || c2 ? 0.f : al, zQ = c1 ? al : be, zR = c1 ? be : (c2 ? al : 0.f);
+  const float iden = __frcp_rn(zQ - zP);
   // f[u,u,v] = e^{iu} G(v - u), e^{i(v-u)} = Pv conj(Pu)
-  auto fuuv = [&](int u, int v) { return cmul(ph[u], Gfun(conjmul(ph[v], ph[u]), z[v] - z[u])); };
-  const cf fRRQ = fuuv(R, Q), fRRP = fuuv(R, P), fQQR = fuuv(Q, R), fPPR = fuuv(P, R);
-  cf D[3];
-  D[R] = cscale(csub(fRRQ, fRRP), iden);
-  D[Q] = cscale(csub(fQQR, d.F), iden);
-  D[P] = cscale(csub(d.F, fPPR), iden);
-  d.Da = D[0]; d.Db = D[1]; d.Dc = D[2];
+  const cf fRRQ = cmul(phR, Gfun(conjmul(phQ, phR), zQ - zR));
+  const cf fRRP = cmul(phR, Gfun(conjmul(phP, phR), zP - zR));
+  const cf fQQR = cmul(phQ, Gfun(conjmul(phR, phQ), zR - zQ));
+  const cf fPPR = cmul(phP, Gfun(conjmul(phR, phP), zR - zP));
+  const cf DR = cscale(csub(fRRQ, fRRP), iden);
+  const cf DQ = cscale(csub(fQQR, d.F), iden);
+  const cf DP = cscale(csub(d.F, fPPR), iden);
+  d.Da = csel(c1 || c2, DP, DR);
+  d.Db = csel(c1, DQ, csel(c2, DR, DP));
+  d.Dc = csel(c1, DR, DQ);
   return d;
 }
 
