@@ -199,8 +199,11 @@ ff_kernel(KGridDev kg, BatchDev b, float2* __restrict__ J, int scale_sqrt_w, con
   const int nrb = (kg.L + R - 1) / R;
   const int ndt = (kg.M + 31) / 32;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  // Warps of a CTA take neighbouring direction blocks at the same radial
+  // block: they see the same radii, so they take the large-spread branch at
+  // the same points of the element loop and reach the tile barriers together.
   const int item = blockIdx.x * FF_WARPS + warp;
-  const int dt = item / nrb, rb = item - dt * nrb;
+  const int rb = item / ndt, dt = item - rb * ndt;
   const int j = dt * 32 + lane;
   const bool active = item < ndt * nrb && j < kg.M;
 
@@ -222,8 +225,7 @@ ff_kernel(KGridDev kg, BatchDev b, float2* __restrict__ J, int scale_sqrt_w, con
       dl = make_float3((float)(e[0] - (double)dh.x), (float)(e[1] - (double)dh.y), (float)(e[2] - (double)dh.z));
     }
   }
-  // radii r = rb + nrb * i: every warp sees small and large k alike, so the
-  // warps of a CTA finish an element tile together.
+  // radii r = rb + nrb * i: every warp sees small and large k alike.
   df km[R];
 #pragma unroll
   for (int i = 0; i < R; ++i) {
