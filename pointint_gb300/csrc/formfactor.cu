@@ -161,30 +161,42 @@ constexpr int FF_CHUNK = 16;  // elements summed in FP32 before the compensated 
 // Sums over thousands of elements: each thread adds FF_CHUNK element terms into
 // a fresh FP32 partial, then adds the partial to a Kahan-compensated running
 // sum, so rounding does not grow with the element count (a plain FP32 sum over
-// 1,280 triangles measured ~1e-6 of max|A| per node).
+// 1,280 triangles measured ~1e-6 of max|A| per node).  The partials live in
+// registers; the running sums and compensations live in shared memory, where
+// they are touched once per FF_CHUNK elements, which leaves the registers for
+// five CTAs per SM.
 template <int R>
 struct Acc {
-  float re[R], im[R];     // current chunk
-  float sre[R], sim[R];   // running sum
-  float cre[R], cim[R];   // Kahan compensation
-  __device__ __forceinline__ void init() {
+  float re[R], im[R];  // current chunk
+  float* run;          // run[(4 i + v) FF_THREADS]: v = sum re, sum im, compensation re, im
+  __device__ __forceinline__ void init(float* base) {
+    run = base + threadIdx.x;
 #pragma unroll
-    for (int i = 0; i < R; ++i) { re[i] = im[i] = sre[i] = sim[i] = cre[i] = cim[i] = 0.f; }
+    for (int i = 0; i < R; ++i) {
+      re[i] = im[i] = 0.f;
+#pragma unroll
+      for (int v = 0; v < 4; ++v) run[(4 * i + v) * FF_THREADS] = 0.f;
+    }
   }
   __device__ __forceinline__ void flush() {
 #pragma unroll
     for (int i = 0; i < R; ++i) {
-      float y = re[i] - cre[i], t = sre[i] + y;
-      cre[i] = (t - sre[i]) - y;
-      sre[i] = t;
-      y = im[i] - cim[i];
-      t = sim[i] + y;
-      cim[i] = (t - sim[i]) - y;
-      sim[i] = t;
+      float* p = run + 4 * i * FF_THREADS;
+      float sre = p[0], sim = p[FF_THREADS], cre = p[2 * FF_THREADS], cim = p[3 * FF_THREADS];
+      float y = re[i] - cre, t = sre + y;
+      cre = (t - sre) - y;
+      sre = t;
+      y = im[i] - cim;
+      t = sim + y;
+      cim = (t - sim) - y;
+      sim = t;
+      p[0] = sre; p[FF_THREADS] = sim; p[2 * FF_THREADS] = cre; p[3 * FF_THREADS] = cim;
       re[i] = 0.f;
       im[i] = 0.f;
     }
   }
+  __device__ __forceinline__ float sre(int i) const { return run[4 * i * FF_THREADS]; }
+  __device__ __forceinline__ float sim(int i) const { return run[(4 * i + 1) * FF_THREADS]; }
 };
 
 // SERVE: blockIdx.y indexes `evals` (serving evaluations: optional rotation of
@@ -233,8 +245,9 @@ ff_kernel(KGridDev kg, BatchDev b, float2* __restrict__ J, int scale_sqrt_w, con
     float2 k = (active && r < kg.L) ? kg.kmag[r] : make_float2(0.f, 0.f);
     km[i] = df{k.x, k.y};
   }
+  __shared__ float run_sm[4 * R * FF_THREADS];
   Acc<R> acc;
-  acc.init();
+  acc.init(run_sm);
 
   __shared__ float4 tile[3 * FF_TILE];
   const int n = od.n_elems;
@@ -341,7 +354,7 @@ ff_kernel(KGridDev kg, BatchDev b, float2* __restrict__ J, int scale_sqrt_w, con
       const int r = rb + nrb * i;
       if (r < kg.L) {
         const int64_t q = (int64_t)r * kg.M + j;
-        cf v{acc.sre[i], acc.sim[i]};
+        cf v{acc.sre(i), acc.sim(i)};
         if (km[i].hi * dnorm < 1e-10f) v = cf{0.f, 0.f};  // A(0) = 0 (affine_dof.cpp:64-65)
         const float sw = kg.sqrtw[q];
         v.re *= sw; v.im *= sw;
@@ -364,7 +377,7 @@ ff_kernel(KGridDev kg, BatchDev b, float2* __restrict__ J, int scale_sqrt_w, con
     const int r = rb + nrb * i;
     if (r < kg.L) {
       const int64_t q = (int64_t)r * kg.M + j;
-      cf v = cmul(cis(df_mul(km[i], so)), cf{acc.sre[i], acc.sim[i]});
+      cf v = cmul(cis(df_mul(km[i], so)), cf{acc.sre(i), acc.sim(i)});
       if (km[i].hi * dnorm < 1e-10f) v = cf{0.f, 0.f};  // A(0) = 0 (affine_dof.cpp:64-65)
       if (scale_sqrt_w) { const float s = kg.sqrtw[q]; v.re *= s; v.im *= s; }
       J[Jrow + q] = make_float2(v.re, v.im);
