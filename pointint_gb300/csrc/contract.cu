@@ -16,6 +16,7 @@
 #include <algorithm>
 #include <mutex>
 #include "pi_internal.h"
+#include "dfmath.cuh"
 
 namespace pi {
 
@@ -120,9 +121,11 @@ __global__ void reduce_tiles_kernel(const float* __restrict__ partials, int nspl
   const int r = e / TB, c = e % TB;
   const int i = bi * TB + r, j = bj * TB + c;
   if (i >= n || j >= n || (bi == bj && r > c)) return;
-  double s = 0.0;
-  for (int sp = 0; sp < nsplit; ++sp) s += (double)partials[((int64_t)sp * npairs + p) * (TB * TB) + e];
-  s *= INV8PI3;
+  // compensated FP32 sum in split order (FP64 adds run at 1/64 of the FP32 rate)
+  kbsum acc{0.f, 0.f};
+#pragma unroll 8
+  for (int sp = 0; sp < nsplit; ++sp) acc.add(__ldcs(partials + ((int64_t)sp * npairs + p) * (TB * TB) + e));
+  const double s = acc.value() * INV8PI3;
   V[(int64_t)i * n + j] = s;
   V[(int64_t)j * n + i] = s;
 }

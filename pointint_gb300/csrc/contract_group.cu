@@ -459,7 +459,7 @@ group_split3_kernel(const GroupDev g, const __grid_constant__ CUtensorMap xmap) 
   }
 }
 
-// Fixed-order FP64 sum of the partial tiles; one thread per (query, i, j) with
+// Fixed-order compensated sum of the partial tiles; one thread per (query, i, j) with
 // i <= j, mirrored.  Grid-stride, so one fixed grid serves every batch.
 __global__ void __launch_bounds__(RED_THREADS) group_reduce_kernel(const GroupDev g) {
   const int64_t n_elems = g.hdr->n_elems;
@@ -482,10 +482,20 @@ __global__ void __launch_bounds__(RED_THREADS) group_reduce_kernel(const GroupDe
     const int64_t off = (int64_t)(i % GM) * GM + (j % GM);
     double s = __longlong_as_double(0x7ff8000000000000LL);  // NaN unless the contraction succeeded
     if (!bad) {
-      s = 0.0;
-      for (int sp = 0; sp < q.nsplit; ++sp)
-        s += (double)g.partials[(q.item0 + (int64_t)sp * npairs + p) * (GM * GM) + off];
-      s *= g.scale / ((double)row_scale(g.rows[q.row0 + i], g.op) * (double)row_scale(g.rows[q.row0 + j], g.op));
+      // compensated FP32 sum in split order; eight loads in flight ahead of their adds
+      const float* src = g.partials + (q.item0 + p) * (GM * GM) + off;
+      const int64_t stride = (int64_t)npairs * (GM * GM);
+      kbsum acc{0.f, 0.f};
+      int sp = 0;
+      for (; sp + 8 <= q.nsplit; sp += 8) {
+        float v[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) v[u] = __ldcs(src + (sp + u) * stride);
+#pragma unroll
+        for (int u = 0; u < 8; ++u) acc.add(v[u]);
+      }
+      for (; sp < q.nsplit; ++sp) acc.add(__ldcs(src + sp * stride));
+      s = acc.value() * g.scale / ((double)row_scale(g.rows[q.row0 + i], g.op) * (double)row_scale(g.rows[q.row0 + j], g.op));
     }
     g.out[q.out_off + (int64_t)i * q.n + j] = s;
     g.out[q.out_off + (int64_t)j * q.n + i] = s;

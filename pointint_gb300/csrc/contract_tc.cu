@@ -28,6 +28,7 @@
 #include <algorithm>
 #include <mutex>
 #include "pi_internal.h"
+#include "dfmath.cuh"
 #include "tc_ptx.cuh"
 
 namespace pi {
@@ -257,10 +258,11 @@ __global__ void reduce_tc_tiles_kernel(const float* __restrict__ partials, int n
   const int r = e / TC_M, c = e % TC_M;
   const int i = bi * TC_M + r, j = bj * TC_M + c;
   if (i >= n || j >= n || (bi == bj && r > c)) return;
-  double s = 0.0;
+  // compensated FP32 sum in split order (FP64 adds run at 1/64 of the FP32 rate)
+  kbsum acc{0.f, 0.f};
 #pragma unroll 8
-  for (int sp = 0; sp < nsplit; ++sp) s += (double)partials[((int64_t)sp * npairs + p) * (TC_M * TC_M) + e];
-  s = (*err != 0) ? __longlong_as_double(0x7ff8000000000000LL) : s * INV8PI3;
+  for (int sp = 0; sp < nsplit; ++sp) acc.add(__ldcs(partials + ((int64_t)sp * npairs + p) * (TC_M * TC_M) + e));
+  const double s = (*err != 0) ? __longlong_as_double(0x7ff8000000000000LL) : acc.value() * INV8PI3;
   V[(int64_t)i * n + j] = s;
   V[(int64_t)j * n + i] = s;
 }

@@ -28,6 +28,20 @@ __device__ __forceinline__ df two_sum(float a, float b) {
   return {s, e};
 }
 
+// Fixed-order compensated FP32 sum (Kahan-Babuska / Neumaier): the running
+// sum and the sum of its rounding errors; hi + lo keeps ~48 bits.  Used for
+// the split-K reductions, where FP64 adds (1/64 of the FP32 rate on GB300)
+// would cost more than reading the partial tiles.
+struct kbsum {
+  float hi, lo;
+  __device__ __forceinline__ void add(float x) {
+    const df t = two_sum(hi, x);
+    hi = t.hi;
+    lo += t.lo;
+  }
+  __device__ __forceinline__ double value() const { return (double)hi + (double)lo; }
+};
+
 __device__ __forceinline__ df quick_two_sum(float a, float b) {  // requires |a| >= |b|
   float s = a + b;
   return {s, b - (s - a)};
