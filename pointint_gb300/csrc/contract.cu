@@ -123,8 +123,17 @@ __global__ void reduce_tiles_kernel(const float* __restrict__ partials, int nspl
   if (i >= n || j >= n || (bi == bj && r > c)) return;
   // compensated FP32 sum in split order (FP64 adds run at 1/64 of the FP32 rate)
   kbsum acc{0.f, 0.f};
-#pragma unroll 8
-  for (int sp = 0; sp < nsplit; ++sp) acc.add(__ldcs(partials + ((int64_t)sp * npairs + p) * (TB * TB) + e));
+  const float* src = partials + (int64_t)p * (TB * TB) + e;
+  const int64_t stride = (int64_t)npairs * (TB * TB);
+  int sp = 0;
+  for (; sp + 16 <= nsplit; sp += 16) {  // sixteen loads in flight ahead of their adds
+    float v[16];
+#pragma unroll
+    for (int u = 0; u < 16; ++u) v[u] = __ldcs(src + (sp + u) * stride);
+#pragma unroll
+    for (int u = 0; u < 16; ++u) acc.add(v[u]);
+  }
+  for (; sp < nsplit; ++sp) acc.add(__ldcs(src + sp * stride));
   const double s = acc.value() * INV8PI3;
   V[(int64_t)i * n + j] = s;
   V[(int64_t)j * n + i] = s;

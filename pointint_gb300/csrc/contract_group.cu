@@ -482,17 +482,17 @@ __global__ void __launch_bounds__(RED_THREADS) group_reduce_kernel(const GroupDe
     const int64_t off = (int64_t)(i % GM) * GM + (j % GM);
     double s = __longlong_as_double(0x7ff8000000000000LL);  // NaN unless the contraction succeeded
     if (!bad) {
-      // compensated FP32 sum in split order; eight loads in flight ahead of their adds
+      // compensated FP32 sum in split order; sixteen loads in flight ahead of their adds
       const float* src = g.partials + (q.item0 + p) * (GM * GM) + off;
       const int64_t stride = (int64_t)npairs * (GM * GM);
       kbsum acc{0.f, 0.f};
       int sp = 0;
-      for (; sp + 8 <= q.nsplit; sp += 8) {
-        float v[8];
+      for (; sp + 16 <= q.nsplit; sp += 16) {
+        float v[16];
 #pragma unroll
-        for (int u = 0; u < 8; ++u) v[u] = __ldcs(src + (sp + u) * stride);
+        for (int u = 0; u < 16; ++u) v[u] = __ldcs(src + (sp + u) * stride);
 #pragma unroll
-        for (int u = 0; u < 8; ++u) acc.add(v[u]);
+        for (int u = 0; u < 16; ++u) acc.add(v[u]);
       }
       for (; sp < q.nsplit; ++sp) acc.add(__ldcs(src + sp * stride));
       s = acc.value() * g.scale / ((double)row_scale(g.rows[q.row0 + i], g.op) * (double)row_scale(g.rows[q.row0 + j], g.op));
