@@ -281,7 +281,7 @@ int pi_compute_Ak_single(const pi_object* obj, const double* k, double* out);
  * as the resident pool (LRU, within hbm_budget_bytes) and the batch arenas have
  * room; each batch runs as one CUDA graph (descriptor upload, form factors of
  * the new rows, one persistent tensor-core contraction over every query of the
- * batch, the FP64 reduction, result download).  Each query's result depends on
+ * batch, the split-K reduction, result download).  Each query's result depends on
  * that query alone, not on the batch it ran in. */
 typedef struct pi_server_s* pi_server;
 
@@ -290,7 +290,7 @@ typedef struct {
   int32_t max_batch_queries; /* 0 = 64 */
   int32_t max_batch_rows;    /* object rows (sum of n over the batch's queries); 0 = 4096 */
   int32_t max_batch_evals;   /* form-factor evaluations per batch; 0 = 256 */
-  int32_t inflight_batches;  /* 1..4; 0 = 2 */
+  int32_t inflight_batches;  /* 1..4; 0 = 4 */
   int32_t precision;         /* PI_CONTRACT_FP16X3 (0 = default) or PI_CONTRACT_BF16X3 */
   int32_t use_graphs;        /* 1: each batch is one CUDA graph launch; 0: plain stream launches; -1 = 1 */
   int32_t autotune;          /* 1: time work-item sizes at creation; 0: built-in sizes; -1 = 1 */

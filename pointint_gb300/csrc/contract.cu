@@ -109,7 +109,7 @@ syrk_fp32_kernel(const float* __restrict__ X, int n, int64_t K, const float* __r
     *reinterpret_cast<float4*>(&out[(ty * 4 + a) * TB + tx * 4]) = make_float4(acc[a][0], acc[a][1], acc[a][2], acc[a][3]);
 }
 
-// Fixed-order FP64 sum of the split partials, scaled by 1/(8 pi^3), mirrored;
+// Fixed-order compensated sum of the split partials, scaled by 1/(8 pi^3), mirrored;
 // one thread per output element of the upper-triangle tiles.
 __global__ void reduce_tiles_kernel(const float* __restrict__ partials, int nsplit, int npairs, int nt, int n,
                                     double* __restrict__ V) {

@@ -15,7 +15,7 @@
 // issues tcgen05.mma (M = N = 128, K = 16) three times per K step and commits
 // each stage back to the producers through an mbarrier.  The epilogue reads
 // the accumulator with tcgen05.ld and writes a per-unit FP32 partial tile;
-// a second kernel sums the partials in a fixed order in FP64.
+// a second kernel sums the partials in a fixed order (compensated FP32).
 //
 // Every wait is bounded (~2 s of SM clock); on expiry the kernel records an
 // error code in the workspace, stops issuing work, drains its outstanding
