@@ -505,6 +505,12 @@ int build_batch(Server& S, Slot& sl, std::vector<cudaEvent_t>* waits) {
     n_elems += out;
   }
   if (sl.n_queries == 0) return 0;
+  // Largest objects first: the evaluation grid's CTAs start in this order, so
+  // a large object's CTAs do not start last and leave the SMs idle at the end
+  // (each evaluation carries its own destination row and row-maximum slots).
+  std::stable_sort(evals, evals + sl.n_evals, [&](const EvalDev& x, const EvalDev& y) {
+    return S.lib->info[x.obj].n_elems > S.lib->info[y.obj].n_elems;
+  });
   hdr->n_items = (int32_t)sl.n_items;
   hdr->n_queries = sl.n_queries;
   hdr->n_elems = n_elems;
