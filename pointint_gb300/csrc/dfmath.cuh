@@ -105,16 +105,17 @@ __device__ __forceinline__ df cdot2(float3 dh, float3 dl, float3 xh, float3 xl) 
 struct cf { float re, im; };
 
 // e^{i (r + q pi/2)} for r in [-pi/4, pi/4]: this project's own least-squares
-// polynomials for sin(r)/r (degree 4 in r^2) and cos(r) (degree 5 in r^2),
-// fitted on Chebyshev-spaced samples of [-pi/4, pi/4]; FP32 evaluation error
-// <= 7e-8 each, about 5x below the hardware sin/cos approximation.  The
+// polynomials for sin(r)/r (degree 3 in r^2) and cos(r) (degree 4 in r^2),
+// fitted on Chebyshev-spaced samples of [-pi/4, pi/4].  Their approximation
+// errors (2.4e-9, 4.7e-11) sit far below FP32 rounding, so the FP32
+// evaluation error is the rounding's, <= 6e-8 each (emulated), about 5x below
+// the hardware sin/cos approximation; one degree more changes nothing.  The
 // quadrant q mod 4 rotates the result.
 __device__ __forceinline__ cf cis_quadrant(float r, int q) {
   const float t = r * r;
-  const float sn = r * fmaf(t, fmaf(t, fmaf(t, fmaf(t, 2.717349162e-06f, -1.983920229e-04f), 8.333329111e-03f),
-                                     -1.666666716e-01f), 1.0f);
-  const float cs = fmaf(t, fmaf(t, fmaf(t, fmaf(t, fmaf(t, -2.717345637e-07f, 2.479892828e-05f), -1.388887991e-03f),
-                                      4.166666791e-02f), -0.5f), 1.0f);
+  const float sn = r * fmaf(t, fmaf(t, fmaf(t, -1.950395963e-04f, 8.332036436e-03f), -1.666665077e-01f), 1.0f);
+  const float cs = fmaf(t, fmaf(t, fmaf(t, fmaf(t, 2.437987678e-05f, -1.388661913e-03f), 4.166661575e-02f), -0.5f),
+                        1.0f);
   q &= 3;
   const float s1 = (q & 1) ? cs : sn;   // sin(r + q pi/2) up to sign
   const float c1 = (q & 1) ? sn : cs;   // cos(r + q pi/2) up to sign
