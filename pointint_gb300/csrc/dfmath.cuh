@@ -116,30 +116,43 @@ __device__ __forceinline__ cf cis_quadrant(float r, int q) {
   const float sn = r * fmaf(t, fmaf(t, fmaf(t, -1.950395963e-04f, 8.332036436e-03f), -1.666665077e-01f), 1.0f);
   const float cs = fmaf(t, fmaf(t, fmaf(t, fmaf(t, 2.437987678e-05f, -1.388661913e-03f), 4.166661575e-02f), -0.5f),
                         1.0f);
-  q &= 3;
   const float s1 = (q & 1) ? cs : sn;   // sin(r + q pi/2) up to sign
   const float c1 = (q & 1) ? sn : cs;   // cos(r + q pi/2) up to sign
-  return {((q + 1) & 2) ? -c1 : c1, (q & 2) ? -s1 : s1};
+  // signs: cos(r + q pi/2) < 0 for q mod 4 = 1, 2 and sin for q mod 4 = 2, 3
+  const unsigned sre = (unsigned)((q + 1) & 2) << 30, sim = (unsigned)(q & 2) << 30;
+  return {__uint_as_float(__float_as_uint(c1) ^ sre), __uint_as_float(__float_as_uint(s1) ^ sim)};
+}
+
+// Round-to-nearest integer of a * b + c, |result| < 2^22, by the 1.5 * 2^23
+// shift: the FMA rounds the exact a * b + c to an integer, returned as a float
+// in *n, and the low bits of the shifted float are that integer modulo 4.
+#define PI_ROUND_SHIFT 12582912.0f
+__device__ __forceinline__ int round_fma(float a, float b, float c, float* n) {
+  const float t = fmaf(a, b, c + PI_ROUND_SHIFT);
+  *n = t - PI_ROUND_SHIFT;
+  return __float_as_int(t);
 }
 
 // e^{i x} for a double-float phase x (|x| < ~1e5): Cody-Waite reduction by
-// pi/2 to r in [-pi/4, pi/4] (fmaf(-n, A, x) is exact: the result needs at
-// most 23 significant bits), then cis_quadrant.
+// pi/2 to r in [-pi/4, pi/4] (n = x.hi 2/pi rounded; fmaf(-n, A, x) is exact:
+// the result needs at most 23 significant bits), then cis_quadrant.
 __device__ __forceinline__ cf cis(df x) {
-  const float n = rintf(x.hi * PI_TWO_OVER_PI);
+  float n;
+  const int q = round_fma(x.hi, PI_TWO_OVER_PI, 0.0f, &n);
   float r = fmaf(-n, PI_PIO2_A, x.hi);
   r = fmaf(-n, PI_PIO2_B, r);
   r += x.lo;
-  return cis_quadrant(r, __float2int_rn(n));
+  return cis_quadrant(r, q);
 }
 
 // e^{2 pi i t} for a phase given in turns, |t| < 2^20: the nearest quarter
 // turn n/4 is removed exactly (t - n/4 needs no more bits than t), and
 // r = 2 pi (t - n/4) lies in [-pi/4, pi/4] up to rounding.
 __device__ __forceinline__ cf cis_turns(float t) {
-  const float n = rintf(4.0f * t);
+  float n;
+  const int q = round_fma(4.0f, t, 0.0f, &n);
   const float r = fmaf(-0.25f, n, t) * 6.283185307179586f;
-  return cis_quadrant(r, __float2int_rn(n));
+  return cis_quadrant(r, q);
 }
 
 __device__ __forceinline__ cf cmul(cf a, cf b) { return {a.re * b.re - a.im * b.im, a.re * b.im + a.im * b.re}; }
