@@ -155,8 +155,9 @@ __global__ void prepare_elems_kernel(const PrepObj* objs, const ObjDev* od, floa
 
 constexpr int FF_THREADS = 128;
 constexpr int FF_WARPS = FF_THREADS / 32;
-constexpr int FF_TILE = 256;  // elements staged per shared-memory tile
+constexpr int FF_TILE = 256;  // elements staged per shared-memory tile (a multiple of FF_CHUNK)
 constexpr int FF_CHUNK = 16;  // elements summed in FP32 before the compensated outer sum
+static_assert(FF_TILE % FF_CHUNK == 0, "element chunks must not straddle tiles");
 
 // Sums over thousands of elements: each thread adds FF_CHUNK element terms into
 // a fresh FP32 partial, then adds the partial to a Kahan-compensated running
@@ -260,7 +261,10 @@ ff_kernel(KGridDev kg, BatchDev b, float2* __restrict__ J, int scale_sqrt_w, con
       for (int t = threadIdx.x; t < 3 * cnt; t += FF_THREADS) tile[t] = src[3 * (int64_t)base + t];
       __syncthreads();
       if (active) {
-        for (int e = 0; e < cnt; ++e) {
+        // chunks of FF_CHUNK elements (tiles hold a multiple of FF_CHUNK)
+        for (int e0 = 0; e0 < cnt; e0 += FF_CHUNK) {
+        const int e1 = min(e0 + FF_CHUNK, cnt);
+        for (int e = e0; e < e1; ++e) {
           const float4 q0 = tile[3 * e], q1 = tile[3 * e + 1], q2 = tile[3 * e + 2];
           const float3 m = make_float3(q0.x, q0.y, q0.z);  // centroid, object frame
           const float3 e1 = make_float3(q1.x, q1.y, q1.z);
@@ -271,6 +275,7 @@ ff_kernel(KGridDev kg, BatchDev b, float2* __restrict__ J, int scale_sqrt_w, con
           const float s1 = fmaf(dh.x, e1.x, fmaf(dh.y, e1.y, dh.z * e1.z));
           const float s2 = fmaf(dh.x, e2.x, fmaf(dh.y, e2.y, dh.z * e2.z));
           const float sp = fmaxf(fmaxf(fabsf(s1), fabsf(s2)), fabsf(s2 - s1));
+          const float kthr = __fdividef(2.0f, sp);  // the series for k sp < 2 (inf when sp = 0)
           const TriPoly tp = tri_series_coeffs(s1, s2, g);
           // vertex phases relative to the centroid (a = m - (e1 + e2)/3, b = a + e1, c = a + e2)
           const float da = -(s1 + s2) * (1.0f / 3.0f), db = da + s1, dc = da + s2;
@@ -279,7 +284,7 @@ ff_kernel(KGridDev kg, BatchDev b, float2* __restrict__ J, int scale_sqrt_w, con
             const float k = km[i].hi;
             const cf P = cis(df_mul_un(km[i], sm));  // centroid phase, double-float
             cf T;
-            if (k * sp < 2.0f) {
+            if (k < kthr) {
               T = tri_series_eval(tp, k);  // centroid Taylor series, gamma folded in
             } else {
               // Large spread: e[pa, pb, pc] = e^{i k.m} e[k da, k db, k dc].  The
@@ -292,7 +297,8 @@ ff_kernel(KGridDev kg, BatchDev b, float2* __restrict__ J, int scale_sqrt_w, con
             acc.re[i] = fmaf(P.re, T.re, fmaf(-P.im, T.im, acc.re[i]));
             acc.im[i] = fmaf(P.re, T.im, fmaf(P.im, T.re, acc.im[i]));
           }
-          if (((base + e) & (FF_CHUNK - 1)) == FF_CHUNK - 1) acc.flush();
+        }
+        if (e1 - e0 == FF_CHUNK) acc.flush();
         }
       }
     }
@@ -310,7 +316,9 @@ ff_kernel(KGridDev kg, BatchDev b, float2* __restrict__ J, int scale_sqrt_w, con
       for (int t = threadIdx.x; t < 2 * cnt; t += FF_THREADS) tile[t] = src[2 * (int64_t)base + t];
       __syncthreads();
       if (active) {
-        for (int e = 0; e < cnt; ++e) {
+        for (int e0 = 0; e0 < cnt; e0 += FF_CHUNK) {
+        const int e1 = min(e0 + FF_CHUNK, cnt);
+        for (int e = e0; e < e1; ++e) {
           const float4 q0 = tile[2 * e], q1 = tile[2 * e + 1];
           const df sc = cdot(dh, dl, make_float3(q0.x, q0.y, q0.z));
           const float sn = dh.x * q1.x + dh.y * q1.y + dh.z * q1.z;  // dir . (A n)
@@ -322,7 +330,7 @@ ff_kernel(KGridDev kg, BatchDev b, float2* __restrict__ J, int scale_sqrt_w, con
             for (int i = 0; i < R; ++i) {
               const float x = km[i].hi * rr;
               const float S = (x < 1e-10f) ? 1.0f : 2.0f * j1x(x);
-              const cf P = cis(df_mul(km[i], sc));
+              const cf P = cis(df_mul_un(km[i], sc));
               const float m = S * amp;
               acc.re[i] = fmaf(m, P.re, acc.re[i]);
               acc.im[i] = fmaf(m, P.im, acc.im[i]);
@@ -333,12 +341,13 @@ ff_kernel(KGridDev kg, BatchDev b, float2* __restrict__ J, int scale_sqrt_w, con
             for (int i = 0; i < R; ++i) {
               const float k2 = km[i].hi * km[i].hi;
               const float m = __expf(hs * k2) * amp;
-              const cf P = cis(df_mul(km[i], sc));
+              const cf P = cis(df_mul_un(km[i], sc));
               acc.re[i] = fmaf(m, P.re, acc.re[i]);
               acc.im[i] = fmaf(m, P.im, acc.im[i]);
             }
           }
-          if (((base + e) & (FF_CHUNK - 1)) == FF_CHUNK - 1) acc.flush();
+        }
+        if (e1 - e0 == FF_CHUNK) acc.flush();
         }
       }
     }
