@@ -241,10 +241,10 @@ __device__ __forceinline__ TriPoly tri_series_coeffs(float s1, float s2, float g
   return t;
 }
 
-__device__ __forceinline__ cf tri_series_eval(const TriPoly& t, float k) {
-  const float u = k * k;
+// u = k^2, k3 = k^3.
+__device__ __forceinline__ cf tri_series_eval(const TriPoly& t, float u, float k3) {
   const float re = fmaf(u, fmaf(u, fmaf(u, fmaf(u, fmaf(u, fmaf(u, t.a[6], t.a[5]), t.a[4]), t.a[3]), t.a[2]), t.a[1]), t.a[0]);
-  const float im = (k * u) * fmaf(u, fmaf(u, fmaf(u, fmaf(u, t.b[4], t.b[3]), t.b[2]), t.b[1]), t.b[0]);
+  const float im = k3 * fmaf(u, fmaf(u, fmaf(u, fmaf(u, t.b[4], t.b[3]), t.b[2]), t.b[1]), t.b[0]);
   return {re, im};
 }
 

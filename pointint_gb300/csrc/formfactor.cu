@@ -166,6 +166,17 @@ static_assert(FF_TILE % FF_CHUNK == 0, "element chunks must not straddle tiles")
 // registers; the running sums and compensations live in shared memory, where
 // they are touched once per FF_CHUNK elements, which leaves the registers for
 // five CTAs per SM.
+// A float4 from shared memory, loaded where it is written in the source: the
+// element loop reads its radius constants each time instead of keeping them
+// in registers across the loop.
+__device__ __forceinline__ float4 ld_shared_f4(const float4* p) {
+  float4 v;
+  asm volatile("ld.shared.v4.f32 {%0, %1, %2, %3}, [%4];"
+               : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w)
+               : "r"((unsigned)__cvta_generic_to_shared(p)));
+  return v;
+}
+
 template <int R>
 struct Acc {
   float re[R], im[R];  // current chunk
@@ -239,13 +250,17 @@ ff_kernel(KGridDev kg, BatchDev b, float2* __restrict__ J, int scale_sqrt_w, con
     }
   }
   // radii r = rb + nrb * i: every warp sees small and large k alike.
-  df km[R];
-#pragma unroll
-  for (int i = 0; i < R; ++i) {
-    int r = rb + nrb * i;
-    float2 k = (active && r < kg.L) ? kg.kmag[r] : make_float2(0.f, 0.f);
-    km[i] = df{k.x, k.y};
+  // The warp's radii as (k hi, k lo, k^2, k^3), in shared memory: every lane
+  // reads the same entry (a broadcast), once per element and radius, which
+  // keeps them out of the registers the element loop needs.
+  __shared__ float4 krad[FF_WARPS][R];
+  if (lane < R) {
+    const int r = rb + nrb * lane;
+    const float2 k = (item < ndt * nrb && r < kg.L) ? kg.kmag[r] : make_float2(0.f, 0.f);
+    krad[warp][lane] = make_float4(k.x, k.y, k.x * k.x, k.x * k.x * k.x);
   }
+  __syncwarp();
+  const float4* kw = krad[warp];
   __shared__ float run_sm[4 * R * FF_THREADS];
   Acc<R> acc;
   acc.init(run_sm);
@@ -281,11 +296,12 @@ ff_kernel(KGridDev kg, BatchDev b, float2* __restrict__ J, int scale_sqrt_w, con
           const float da = -(s1 + s2) * (1.0f / 3.0f), db = da + s1, dc = da + s2;
 #pragma unroll
           for (int i = 0; i < R; ++i) {
-            const float k = km[i].hi;
-            const cf P = cis(df_mul_un(km[i], sm));  // centroid phase, double-float
+            const float4 kr = ld_shared_f4(kw + i);
+            const float k = kr.x;
+            const cf P = cis(df_mul_un(df{kr.x, kr.y}, sm));  // centroid phase, double-float
             cf T;
             if (k < kthr) {
-              T = tri_series_eval(tp, k);  // centroid Taylor series, gamma folded in
+              T = tri_series_eval(tp, kr.z, kr.w);  // centroid Taylor series, gamma folded in
             } else {
               // Large spread: e[pa, pb, pc] = e^{i k.m} e[k da, k db, k dc].  The
               // relative phases are FP32 products: their error |k d| 6e-8 rad
@@ -328,9 +344,10 @@ ff_kernel(KGridDev kg, BatchDev b, float2* __restrict__ J, int scale_sqrt_w, con
             const float rr = q0.w * sqrtf(perp);                    // rho |k'_perp| / kmag
 #pragma unroll
             for (int i = 0; i < R; ++i) {
-              const float x = km[i].hi * rr;
+              const float4 kr = ld_shared_f4(kw + i);
+              const float x = kr.x * rr;
               const float S = (x < 1e-10f) ? 1.0f : 2.0f * j1x(x);
-              const cf P = cis(df_mul_un(km[i], sc));
+              const cf P = cis(df_mul_un(df{kr.x, kr.y}, sc));
               const float m = S * amp;
               acc.re[i] = fmaf(m, P.re, acc.re[i]);
               acc.im[i] = fmaf(m, P.im, acc.im[i]);
@@ -339,9 +356,9 @@ ff_kernel(KGridDev kg, BatchDev b, float2* __restrict__ J, int scale_sqrt_w, con
             const float hs = -0.5f * q0.w * q0.w * perp;
 #pragma unroll
             for (int i = 0; i < R; ++i) {
-              const float k2 = km[i].hi * km[i].hi;
-              const float m = __expf(hs * k2) * amp;
-              const cf P = cis(df_mul_un(km[i], sc));
+              const float4 kr = ld_shared_f4(kw + i);
+              const float m = __expf(hs * kr.z) * amp;
+              const cf P = cis(df_mul_un(df{kr.x, kr.y}, sc));
               acc.re[i] = fmaf(m, P.re, acc.re[i]);
               acc.im[i] = fmaf(m, P.im, acc.im[i]);
             }
@@ -364,7 +381,7 @@ ff_kernel(KGridDev kg, BatchDev b, float2* __restrict__ J, int scale_sqrt_w, con
       if (r < kg.L) {
         const int64_t q = (int64_t)r * kg.M + j;
         cf v{acc.sre(i), acc.sim(i)};
-        if (km[i].hi * dnorm < 1e-10f) v = cf{0.f, 0.f};  // A(0) = 0 (affine_dof.cpp:64-65)
+        if (kw[i].x * dnorm < 1e-10f) v = cf{0.f, 0.f};  // A(0) = 0 (affine_dof.cpp:64-65)
         const float sw = kg.sqrtw[q];
         v.re *= sw; v.im *= sw;
         ev.dst[(int64_t)j * kg.L + r] = make_float2(v.re, v.im);
@@ -386,8 +403,8 @@ ff_kernel(KGridDev kg, BatchDev b, float2* __restrict__ J, int scale_sqrt_w, con
     const int r = rb + nrb * i;
     if (r < kg.L) {
       const int64_t q = (int64_t)r * kg.M + j;
-      cf v = cmul(cis(df_mul(km[i], so)), cf{acc.sre(i), acc.sim(i)});
-      if (km[i].hi * dnorm < 1e-10f) v = cf{0.f, 0.f};  // A(0) = 0 (affine_dof.cpp:64-65)
+      cf v = cmul(cis(df_mul(df{kw[i].x, kw[i].y}, so)), cf{acc.sre(i), acc.sim(i)});
+      if (kw[i].x * dnorm < 1e-10f) v = cf{0.f, 0.f};  // A(0) = 0 (affine_dof.cpp:64-65)
       if (scale_sqrt_w) { const float s = kg.sqrtw[q]; v.re *= s; v.im *= s; }
       J[Jrow + q] = make_float2(v.re, v.im);
     }
