@@ -104,6 +104,15 @@ __device__ __forceinline__ df cdot2(float3 dh, float3 dl, float3 xh, float3 xl) 
 
 struct cf { float re, im; };
 
+// 1/x by the hardware approximation (rcp.approx.ftz: about 1 ulp, inf at 0).
+// Used where the result scales a difference that already carries far more
+// rounding error than that, as in the divided differences below.
+__device__ __forceinline__ float rcp_fast(float x) {
+  float r;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+
 // e^{i (r + q pi/2)} for r in [-pi/4, pi/4]: this project's own least-squares
 // polynomials for sin(r)/r (degree 3 in r^2) and cos(r) (degree 4 in r^2),
 // fitted on Chebyshev-spaced samples of [-pi/4, pi/4].  Their approximation
@@ -208,7 +217,9 @@ __device__ __forceinline__ cf tri_series(float al, float be) {
 // nu H_{m-3}, and
 //   Re S = sum_j a_j u^j (u = k^2),   Im S = k^3 sum_j b_j u^j.
 // tri_series_coeffs returns g * a_0..a_6 and g * b_0..b_4 so that one radius
-// costs two Horner chains.
+// costs two Horner chains.  The factorials enter as constant reciprocals
+// (1.0f / c folds at compile time): g / c would be an IEEE division per
+// coefficient.
 struct TriPoly { float a[7], b[5]; };
 
 __device__ __forceinline__ TriPoly tri_series_coeffs(float s1, float s2, float g) {
@@ -227,17 +238,17 @@ __device__ __forceinline__ TriPoly tri_series_coeffs(float s1, float s2, float g
   const float H12 = fmaf(mu, H10, nu * H9);
   TriPoly t;
   t.a[0] = -0.5f * g;
-  t.a[1] = H2 * (g / 24.0f);
-  t.a[2] = -H4 * (g / 720.0f);
-  t.a[3] = H6 * (g / 40320.0f);
-  t.a[4] = -H8 * (g / 3628800.0f);
-  t.a[5] = H10 * (g / 479001600.0f);
-  t.a[6] = -H12 * (g / 87178291200.0f);
-  t.b[0] = H3 * (g / 120.0f);
-  t.b[1] = -H5 * (g / 5040.0f);
-  t.b[2] = H7 * (g / 362880.0f);
-  t.b[3] = -H9 * (g / 39916800.0f);
-  t.b[4] = H11 * (g / 6227020800.0f);
+  t.a[1] = H2 * (g * (1.0f / 24.0f));
+  t.a[2] = -H4 * (g * (1.0f / 720.0f));
+  t.a[3] = H6 * (g * (1.0f / 40320.0f));
+  t.a[4] = -H8 * (g * (1.0f / 3628800.0f));
+  t.a[5] = H10 * (g * (1.0f / 479001600.0f));
+  t.a[6] = -H12 * (g * (1.0f / 87178291200.0f));
+  t.b[0] = H3 * (g * (1.0f / 120.0f));
+  t.b[1] = -H5 * (g * (1.0f / 5040.0f));
+  t.b[2] = H7 * (g * (1.0f / 362880.0f));
+  t.b[3] = -H9 * (g * (1.0f / 39916800.0f));
+  t.b[4] = H11 * (g * (1.0f / 6227020800.0f));
   return t;
 }
 
@@ -254,7 +265,7 @@ __device__ __forceinline__ cf tri_series_eval(const TriPoly& t, float u, float k
 // cos, sin and sinc on |g/2| < 1/4 (truncation < 1e-9).  Both forms are
 // evaluated and one is selected, so the lanes of a warp never split on |g|.
 __device__ __forceinline__ cf dd1(cf Pu, cf Pv, float g) {
-  const float ig = __frcp_rn(g);  // inf for g = 0, where the series form is taken
+  const float ig = rcp_fast(g);  // inf for g = 0, where the series form is taken
   const cf big = cscale(csub(Pv, Pu), ig);
   const float x = 0.5f * g, x2 = x * x;
   const float c = fmaf(x2, fmaf(x2, fmaf(x2, -1.0f / 720.0f, 1.0f / 24.0f), -0.5f), 1.0f);
@@ -285,7 +296,7 @@ __device__ __forceinline__ cf tri_generic(cf Pa, cf Pb, cf Pc, float al, float b
   const float g2 = c1 ? gac : (c2 ? gab : -gab);
   const float den = c1 ? gab : (c2 ? gac : gbc);
   const cf fRQ = dd1(u1, v1, g1), fPR = dd1(u2, v2, g2);
-  const float s = __frcp_rn(den);
+  const float s = rcp_fast(den);
   return {(fRQ.re - fPR.re) * s, (fRQ.im - fPR.im) * s};
 }
 

@@ -72,7 +72,7 @@ __device__ __forceinline__ TriDer tri_series_der(cf P, float al, float be) {
 // Both are evaluated and one is selected (no divergent branch).
 __device__ __forceinline__ cf Gfun(cf E, float h) {
   const float h2 = h * h;
-  const float ih2 = __frcp_rn(h2);  // inf for h = 0, where the series is taken
+  const float ih2 = rcp_fast(h2);  // inf for h = 0, where the series is taken
   const float re = fmaf(h2, fmaf(h2, fmaf(h2, fmaf(h2, -1.0f / 3628800.0f, 1.0f / 40320.0f), -1.0f / 720.0f),
                                  1.0f / 24.0f), -0.5f);
   const float im = h * fmaf(h2, fmaf(h2, fmaf(h2, fmaf(h2, -1.0f / 39916800.0f, 1.0f / 362880.0f), -1.0f / 5040.0f),
@@ -97,7 +97,7 @@ __device__ __forceinline__ TriDer tri_generic_der(cf Pa, cf Pb, cf Pc, float al,
   // vertices as (phasor, relative phase): a = 0, b = al, c = be
   const cf phP = csel(c1 || c2, Pa, Pb), phQ = csel(c1, Pb, Pc), phR = csel(c1, Pc, csel(c2, Pb, Pa));
   const float zP = c1 || c2 ? 0.f : al, zQ = c1 ? al : be, zR = c1 ? be : (c2 ? al : 0.f);
-  const float iden = __frcp_rn(zQ - zP);
+  const float iden = rcp_fast(zQ - zP);
   // f[u,u,v] = e^{iu} G(v - u), e^{i(v-u)} = Pv conj(Pu)
   const cf fRRQ = cmul(phR, Gfun(conjmul(phQ, phR), zQ - zR));
   const cf fRRP = cmul(phR, Gfun(conjmul(phP, phR), zP - zR));
