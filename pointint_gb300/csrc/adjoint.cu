@@ -178,7 +178,7 @@ adj_surf_kernel(KGridDev kg, BatchDev b, const AdjWork* __restrict__ work, const
       const df sc = cdot(dh, dl, c);
       const float sn = dh.x * nn.x + dh.y * nn.y + dh.z * nn.z;
       const float perp = fmaxf(st.qd[jj] - sn * sn, 0.f);
-      const float rr = p0 * sqrtf(perp);
+      const float rr = p0 * sqrt_fast(perp);
       const float amp = sn * inv_norm;
       float s_c = 0.f, s_n = 0.f, s_m = 0.f;
       const float2* Bj = st.B + jj * ADJ_LMAX;

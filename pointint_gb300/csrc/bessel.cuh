@@ -40,7 +40,7 @@ __device__ __forceinline__ float horner7(const float* c, float s) {
 // J_nu(x) sqrt(x) for x >= 8 (nu = 1 or 2): sqrt(2/pi) (P cos chi - Q sin chi).
 __device__ __forceinline__ float hankel_scaled(float x, const float* P, const float* Q, float phase_hi,
                                                float phase_lo) {
-  const float ix = __frcp_rn(x);
+  const float ix = rcp_fast(x);
   const float s = 64.0f * ix * ix;
   const float p = horner7(P, s);
   const float q = horner7(Q, s) * 8.0f * ix;
@@ -59,7 +59,7 @@ __device__ __forceinline__ float j1x(float x) {
                       1.892280608e-07f, -4.536089548e-08f, 7.152803683e-09f};
   if (x < 8.0f) return clenshaw12(c, fmaf(x * x, 2.0f / 64.0f, -1.0f));
   // 3 pi / 4 = 2.35619449019234492885 -> FP32 hi + lo
-  return hankel_scaled(x, P, Q, 2.356194496154785f, -5.962440319e-09f) * rsqrtf(x) / x;
+  return hankel_scaled(x, P, Q, 2.356194496154785f, -5.962440319e-09f) * rsqrtf(x) * rcp_fast(x);
 }
 
 __device__ __forceinline__ float j2x2(float x) {
@@ -72,7 +72,7 @@ __device__ __forceinline__ float j2x2(float x) {
                       -2.668556647e-07f, 6.115627116e-08f, -9.458235084e-09f};
   if (x < 8.0f) return clenshaw12(c, fmaf(x * x, 2.0f / 64.0f, -1.0f));
   // 5 pi / 4 = 3.92699081698724154808 -> FP32 hi + lo
-  const float ix = __frcp_rn(x);
+  const float ix = rcp_fast(x);
   return hankel_scaled(x, P, Q, 3.9269907474517822f, 6.953546006e-08f) * rsqrtf(x) * ix * ix;
 }
 

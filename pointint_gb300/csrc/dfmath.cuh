@@ -113,6 +113,15 @@ __device__ __forceinline__ float rcp_fast(float x) {
   return r;
 }
 
+// sqrt(x) by the hardware approximation (sqrt.approx.ftz: about 1 ulp), for
+// arguments of Bessel functions and the like, where an IEEE square root's
+// multi-instruction sequence buys nothing.
+__device__ __forceinline__ float sqrt_fast(float x) {
+  float r;
+  asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+
 // e^{i (r + q pi/2)} for r in [-pi/4, pi/4]: this project's own least-squares
 // polynomials for sin(r)/r (degree 3 in r^2) and cos(r) (degree 4 in r^2),
 // fitted on Chebyshev-spaced samples of [-pi/4, pi/4].  Their approximation

@@ -341,7 +341,7 @@ ff_kernel(KGridDev kg, BatchDev b, float2* __restrict__ J, int scale_sqrt_w, con
           const float perp = fmaxf(qd - sn * sn, 0.f);              // |k'_perp|^2 / kmag^2
           const float amp = sn * inv_norm * q1.w;                   // area|w * (k'.n)/|k|
           if (disk) {
-            const float rr = q0.w * sqrtf(perp);                    // rho |k'_perp| / kmag
+            const float rr = q0.w * sqrt_fast(perp);                // rho |k'_perp| / kmag
 #pragma unroll
             for (int i = 0; i < R; ++i) {
               const float4 kr = ld_shared_f4(kw + i);

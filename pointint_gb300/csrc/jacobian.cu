@@ -269,7 +269,7 @@ jac_affine_surf_kernel(KGridDev kg, BatchDev b, const JacObj* __restrict__ jobs,
       const cf P = cis(df_mul_un(t.k, sc));
       float S, Sr;
       if (disk) {
-        const float x = k * q0.w * sqrtf(perp);
+        const float x = k * q0.w * sqrt_fast(perp);
         S = q1.w * ((x < 1e-10f) ? 1.0f : 2.0f * j1x(x));
         Sr = -2.0f * q1.w * q0.w * q0.w * j2x2(x);
       } else {
