@@ -83,6 +83,15 @@ __device__ __forceinline__ df cdot(float3 dh, float3 dl, float3 x) {
   return quick_two_sum(t.hi, lo);
 }
 
+// cdot without the final renormalisation: (hi, lo) with |lo| a few ulp of
+// hi, enough for df_mul_un and cis, which treat the two parts separately.
+__device__ __forceinline__ df cdot_un(float3 dh, float3 dl, float3 x) {
+  df p0 = two_prod(dh.x, x.x), p1 = two_prod(dh.y, x.y), p2 = two_prod(dh.z, x.z);
+  df s = two_sum(p0.hi, p1.hi);
+  df t = two_sum(s.hi, p2.hi);
+  return {t.hi, s.lo + t.lo + p0.lo + p1.lo + p2.lo + (dl.x * x.x + dl.y * x.y + dl.z * x.z)};
+}
+
 // (dh + dl) . (xh + xl) in double-float; the dl . xl term (~2^-48 relative)
 // is dropped.
 __device__ __forceinline__ df cdot2(float3 dh, float3 dl, float3 xh, float3 xl) {
@@ -137,7 +146,9 @@ __device__ __forceinline__ cf cis_quadrant(float r, int q) {
   const float s1 = (q & 1) ? cs : sn;   // sin(r + q pi/2) up to sign
   const float c1 = (q & 1) ? sn : cs;   // cos(r + q pi/2) up to sign
   // signs: cos(r + q pi/2) < 0 for q mod 4 = 1, 2 and sin for q mod 4 = 2, 3
-  const unsigned sre = (unsigned)((q + 1) & 2) << 30, sim = (unsigned)(q & 2) << 30;
+  // ((q + 1) & 2) = (q & 2) ^ ((q & 1) << 1), so the cosine's sign bit is the
+  // sine's flipped by q's low bit
+  const unsigned sim = (unsigned)(q & 2) << 30, sre = sim ^ ((unsigned)q << 31);
   return {__uint_as_float(__float_as_uint(c1) ^ sre), __uint_as_float(__float_as_uint(s1) ^ sim)};
 }
 
@@ -236,28 +247,30 @@ __device__ __forceinline__ TriPoly tri_series_coeffs(float s1, float s2, float g
   const float db = s1 + da, dc = s2 + da;
   const float mu = 0.5f * (da * da + db * db + dc * dc);
   const float nu = da * db * dc;
-  const float H2 = mu, H3 = nu, H4 = mu * H2;
-  const float H5 = fmaf(mu, H3, nu * H2);
-  const float H6 = fmaf(mu, H4, nu * H3);
-  const float H7 = fmaf(mu, H5, nu * H4);
-  const float H8 = fmaf(mu, H6, nu * H5);
-  const float H9 = fmaf(mu, H7, nu * H6);
-  const float H10 = fmaf(mu, H8, nu * H7);
-  const float H11 = fmaf(mu, H9, nu * H8);
-  const float H12 = fmaf(mu, H10, nu * H9);
+  // G_m = g H_m: the recurrence is linear, so starting it from g H_2, g H_3
+  // leaves one constant multiply per coefficient
+  const float G2 = mu * g, G3 = nu * g, G4 = mu * G2;
+  const float G5 = fmaf(mu, G3, nu * G2);
+  const float G6 = fmaf(mu, G4, nu * G3);
+  const float G7 = fmaf(mu, G5, nu * G4);
+  const float G8 = fmaf(mu, G6, nu * G5);
+  const float G9 = fmaf(mu, G7, nu * G6);
+  const float G10 = fmaf(mu, G8, nu * G7);
+  const float G11 = fmaf(mu, G9, nu * G8);
+  const float G12 = fmaf(mu, G10, nu * G9);
   TriPoly t;
   t.a[0] = -0.5f * g;
-  t.a[1] = H2 * (g * (1.0f / 24.0f));
-  t.a[2] = -H4 * (g * (1.0f / 720.0f));
-  t.a[3] = H6 * (g * (1.0f / 40320.0f));
-  t.a[4] = -H8 * (g * (1.0f / 3628800.0f));
-  t.a[5] = H10 * (g * (1.0f / 479001600.0f));
-  t.a[6] = -H12 * (g * (1.0f / 87178291200.0f));
-  t.b[0] = H3 * (g * (1.0f / 120.0f));
-  t.b[1] = -H5 * (g * (1.0f / 5040.0f));
-  t.b[2] = H7 * (g * (1.0f / 362880.0f));
-  t.b[3] = -H9 * (g * (1.0f / 39916800.0f));
-  t.b[4] = H11 * (g * (1.0f / 6227020800.0f));
+  t.a[1] = G2 * (1.0f / 24.0f);
+  t.a[2] = G4 * (-1.0f / 720.0f);
+  t.a[3] = G6 * (1.0f / 40320.0f);
+  t.a[4] = G8 * (-1.0f / 3628800.0f);
+  t.a[5] = G10 * (1.0f / 479001600.0f);
+  t.a[6] = G12 * (-1.0f / 87178291200.0f);
+  t.b[0] = G3 * (1.0f / 120.0f);
+  t.b[1] = G5 * (-1.0f / 5040.0f);
+  t.b[2] = G7 * (1.0f / 362880.0f);
+  t.b[3] = G9 * (-1.0f / 39916800.0f);
+  t.b[4] = G11 * (1.0f / 6227020800.0f);
   return t;
 }
 

@@ -286,7 +286,7 @@ ff_kernel(KGridDev kg, BatchDev b, float2* __restrict__ J, int scale_sqrt_w, con
           const float3 e2 = make_float3(q2.x, q2.y, q2.z);
           // -2 (khat . S): gamma of the reference times the -2 of Phi = -2 e[..]
           const float g = -2.0f * (dh.x * q0.w + dh.y * q1.w + dh.z * q2.w) * inv_norm;
-          const df sm = cdot(dh, dl, m);
+          const df sm = cdot_un(dh, dl, m);
           const float s1 = fmaf(dh.x, e1.x, fmaf(dh.y, e1.y, dh.z * e1.z));
           const float s2 = fmaf(dh.x, e2.x, fmaf(dh.y, e2.y, dh.z * e2.z));
           const float sp = fmaxf(fmaxf(fabsf(s1), fabsf(s2)), fabsf(s2 - s1));
@@ -336,7 +336,7 @@ ff_kernel(KGridDev kg, BatchDev b, float2* __restrict__ J, int scale_sqrt_w, con
         const int e1 = min(e0 + FF_CHUNK, cnt);
         for (int e = e0; e < e1; ++e) {
           const float4 q0 = tile[2 * e], q1 = tile[2 * e + 1];
-          const df sc = cdot(dh, dl, make_float3(q0.x, q0.y, q0.z));
+          const df sc = cdot_un(dh, dl, make_float3(q0.x, q0.y, q0.z));
           const float sn = dh.x * q1.x + dh.y * q1.y + dh.z * q1.z;  // dir . (A n)
           const float perp = fmaxf(qd - sn * sn, 0.f);              // |k'_perp|^2 / kmag^2
           const float amp = sn * inv_norm * q1.w;                   // area|w * (k'.n)/|k|
