@@ -218,7 +218,7 @@ adj_surf_kernel(KGridDev kg, BatchDev b, const AdjWork* __restrict__ work, const
 }
 
 // Per triangle: 9 outputs dL/dv0, dL/dv1, dL/dv2 (world-frame vertex positions).
-__global__ void __launch_bounds__(ADJ_THREADS)
+__global__ void __launch_bounds__(ADJ_THREADS, 4)
 adj_tri_kernel(KGridDev kg, BatchDev b, const AdjWork* __restrict__ work, const float2* __restrict__ Bw,
                float* __restrict__ out) {
   __shared__ AdjStage st;
@@ -251,21 +251,37 @@ adj_tri_kernel(KGridDev kg, BatchDev b, const AdjWork* __restrict__ work, const 
       const df sa = df_add(sm, df_div3(df_add(d1, d2)) * -1.0f);
       const df sb = df_add(sa, d1), sc = df_add(sa, d2);
       const float sp = fmaxf(fmaxf(fabsf(d1.hi), fabsf(d2.hi)), fabsf(d2.hi - d1.hi));
+      const float kthr = __fdividef(2.0f, sp);  // the series for k sp < 2 (inf when sp = 0)
       const float gam = (dh.x * S.x + dh.y * S.y + dh.z * S.z) * inv_norm;
+      const TriDerPoly cp = tri_der_coeffs(d1.hi, d2.hi);
       float t0 = 0.f, ta = 0.f, tb = 0.f, tc = 0.f;
       const float2* Bj = st.B + jj * ADJ_LMAX;
       for (int r = 0; r < kg.L; ++r) {
         const float2 Bv = Bj[r];
         const df k = df{km[r].x, km[r].y};
-        const float al = k.hi * d1.hi, be = k.hi * d2.hi;
-        TriDer d;
-        if (k.hi * sp < 2.0f) d = tri_series_der(cis(df_mul_un(k, sm)), al, be);
-        else d = tri_generic_der_at(k, sa, sb, sc, al, be);
-        // Re(conj(B) X) = B.re X.re + B.im X.im
-        t0 = fmaf(Bv.x, d.F.re, fmaf(Bv.y, d.F.im, t0));
-        ta = fmaf(k.hi, fmaf(Bv.x, d.Da.re, Bv.y * d.Da.im), ta);
-        tb = fmaf(k.hi, fmaf(Bv.x, d.Db.re, Bv.y * d.Db.im), tb);
-        tc = fmaf(k.hi, fmaf(Bv.x, d.Dc.re, Bv.y * d.Dc.im), tc);
+        if (k.hi < kthr) {
+          // F = P SF, D_v = P SV with the series as polynomials in k; with
+          // BP = conj(B) P, Re(conj(B) X) = Re(BP SX) and D_a = i F - D_b - D_c
+          const cf P = cis(df_mul_un(k, sm));
+          const float u = k.hi * k.hi, k3 = u * k.hi;
+          const float fre = poly_u(cp.fa, u), fim = k3 * poly_u(cp.fb, u);
+          const float bim = poly_u(cp.ba, u), bre = k.hi * poly_u(cp.bb, u);
+          const float cim = poly_u(cp.ca, u), cre = k.hi * poly_u(cp.cb, u);
+          const float pr = fmaf(Bv.x, P.re, Bv.y * P.im), pi = fmaf(Bv.x, P.im, -Bv.y * P.re);
+          const float f_re = fmaf(pr, fre, -pi * fim), f_im = fmaf(pr, fim, pi * fre);
+          const float b_re = fmaf(pr, bre, -pi * bim), c_re = fmaf(pr, cre, -pi * cim);
+          t0 += f_re;
+          ta = fmaf(k.hi, -f_im - b_re - c_re, ta);
+          tb = fmaf(k.hi, b_re, tb);
+          tc = fmaf(k.hi, c_re, tc);
+        } else {
+          const TriDer d = tri_generic_der_at(k, sa, sb, sc, k.hi * d1.hi, k.hi * d2.hi);
+          // Re(conj(B) X) = B.re X.re + B.im X.im
+          t0 = fmaf(Bv.x, d.F.re, fmaf(Bv.y, d.F.im, t0));
+          ta = fmaf(k.hi, fmaf(Bv.x, d.Da.re, Bv.y * d.Da.im), ta);
+          tb = fmaf(k.hi, fmaf(Bv.x, d.Db.re, Bv.y * d.Db.im), tb);
+          tc = fmaf(k.hi, fmaf(Bv.x, d.Dc.re, Bv.y * d.Dc.im), tc);
+        }
       }
       // khat x u / 2 terms for grad gamma
       const float3 kh = make_float3(dh.x * inv_norm, dh.y * inv_norm, dh.z * inv_norm);

@@ -65,6 +65,64 @@ __device__ __forceinline__ TriDer tri_series_der(cf P, float al, float be) {
   return d;
 }
 
+// The small-spread series of F, D_b and D_c as polynomials in the radius k
+// for one element and direction, so that each radius costs a few Horner
+// chains instead of the recurrences of tri_series_der.  With the centred
+// direction dots d_v (centred phases k d_v), h_m = k^m H_m and
+// h^(v)_m = k^m H^(v)_m, H^(v)_m = H_m + d_v H^(v)_{m-1}, H^(v)_0 = 1, so with
+// u = k^2 (P = e^{i pm} applied outside):
+//   Re F/P = sum_j fa_j u^j,        fa_j = (-1)^(j+1) H_2j / (2j+2)!
+//   Im F/P = k^3 sum_j fb_j u^j,    fb_j = (-1)^j H_(2j+3) / (2j+5)!
+//   Im D_v/P = sum_j va_j u^j,      va_j = (-1)^(j+1) H^(v)_2j / (2j+3)!
+//   Re D_v/P = k sum_j vb_j u^j,    vb_j = (-1)^j H^(v)_(2j+1) / (2j+4)!
+// (m <= 12 as in tri_series_der.)
+struct TriDerPoly { float fa[7], fb[5], ba[7], bb[6], ca[7], cb[6]; };
+
+// c_0 + c_1 u + ... + c_{N-1} u^{N-1} by Horner's rule.
+template <int N>
+__device__ __forceinline__ float poly_u(const float (&c)[N], float u) {
+  float r = c[N - 1];
+#pragma unroll
+  for (int i = N - 2; i >= 0; --i) r = fmaf(r, u, c[i]);
+  return r;
+}
+
+__device__ __forceinline__ TriDerPoly tri_der_coeffs(float s1, float s2) {
+  const float da = -(s1 + s2) * (1.0f / 3.0f);
+  const float db = s1 + da, dc = s2 + da;
+  const float mu = 0.5f * (da * da + db * db + dc * dc);
+  const float nu = da * db * dc;
+  float H[13];
+  H[0] = 1.f; H[1] = 0.f; H[2] = mu; H[3] = nu;
+#pragma unroll
+  for (int m = 4; m <= 12; ++m) H[m] = fmaf(mu, H[m - 2], nu * H[m - 3]);
+  // 1/n! for n = 0..15
+  const float inv_fact[16] = {1.f, 1.f, 0.5f, 1.f / 6, 1.f / 24, 1.f / 120, 1.f / 720, 1.f / 5040, 1.f / 40320,
+                              1.f / 362880, 1.f / 3628800, 1.f / 39916800, 1.f / 479001600, 1.f / 6227020800.f,
+                              1.f / 87178291200.f, 1.f / 1307674368000.f};
+  TriDerPoly c;
+#pragma unroll
+  for (int j = 0; j <= 6; ++j) c.fa[j] = ((j & 1) ? H[2 * j] : -H[2 * j]) * inv_fact[2 * j + 2];
+#pragma unroll
+  for (int j = 0; j <= 4; ++j) c.fb[j] = ((j & 1) ? -H[2 * j + 3] : H[2 * j + 3]) * inv_fact[2 * j + 5];
+  float hb = 1.f, hc = 1.f;  // H^(b)_m, H^(c)_m
+#pragma unroll
+  for (int m = 0; m <= 12; ++m) {
+    if (m > 0) { hb = fmaf(db, hb, H[m]); hc = fmaf(dc, hc, H[m]); }
+    const int j = m >> 1;
+    if ((m & 1) == 0) {
+      const float f = ((j & 1) ? 1.f : -1.f) * inv_fact[m + 3];
+      c.ba[j] = hb * f;
+      c.ca[j] = hc * f;
+    } else {
+      const float f = ((j & 1) ? -1.f : 1.f) * inv_fact[m + 3];
+      c.bb[j] = hb * f;
+      c.cb[j] = hc * f;
+    }
+  }
+  return c;
+}
+
 // G(h) = (e^{ih} - 1 - ih)/h^2 given E = e^{ih}: the direct form for
 // |h| >= 1/2, otherwise the series sum_m i^{m+2} h^m/(m+2)!, m = 0..9:
 //   Re = -1/2 + h^2/24 - h^4/720 + h^6/40320 - h^8/3628800
