@@ -9,8 +9,8 @@
 // K slab into a fresh block before adding it, Kahan-compensated, to its
 // running sum (off-diagonal entries are small differences of large slab sums).
 // Per-split partial tiles are
-// reduced in a fixed order in FP64 by a second kernel: results are bitwise
-// reproducible run to run.
+// reduced in a fixed order (compensated FP32, ~48 bits) by a second kernel:
+// results are bitwise reproducible run to run.
 #include <cuda_runtime.h>
 #include <cstdint>
 #include <algorithm>

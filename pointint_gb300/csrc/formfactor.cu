@@ -9,12 +9,14 @@
 //    its AffineDoF / TriangleMeshDoF into an FP32 object-local frame (origin =
 //    centroid of the transformed anchors); the origin phase e^{ik.o} is applied
 //    per output in double-float.
-//  * ff_kernel: one CTA = one object x (8 warps); a warp owns 32 directions
+//  * ff_kernel: one CTA = one object x 4 warps; a warp owns 32 directions
 //    (one per lane) x R radial nodes of the factored k-grid, so each element's
-//    direction dot products are formed once and reused for R radii.  Elements
-//    are staged through shared memory and read as broadcasts; accumulation
-//    stays in registers (no reduction across threads); each output element is
-//    written once, coalesced, in the contraction's operand layout.
+//    direction dot products and series coefficients are formed once and
+//    reused for R radii.  Elements are staged through shared memory and read
+//    as broadcasts; each thread accumulates its own outputs (no reduction
+//    across threads), 16-element partials in registers and compensated
+//    running sums in shared memory; each output element is written once,
+//    coalesced, in the contraction's operand layout.
 #include <cuda_runtime.h>
 #include <cstdint>
 #include <algorithm>

@@ -12,8 +12,8 @@
 // running at the same time read the same chunks of a tile (one DRAM read, the
 // other pairs hit L2) and neighbouring chunks of each row (long DRAM runs).
 // Each work item writes a 128 x 128 FP32 partial tile, and the reduction sums
-// the partials of every pair in a fixed order in FP64: a query's result does
-// not depend on which other queries share the launch.
+// the partials of every pair in a fixed order (compensated FP32): a query's
+// result does not depend on which other queries share the launch.
 //
 // All counts live in device memory (GHeader), so a launch sequence captured
 // once in a CUDA graph serves every batch.
