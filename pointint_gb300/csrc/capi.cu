@@ -270,14 +270,16 @@ int pi_batch_create(const pi_object* objs, int n, int on_device, pi_stream strea
                             cudaMemcpyDeviceToDevice, s);
     }
   } else {
-    std::vector<unsigned char> hs(std::max<size_t>(src_bytes, 16));
+    // elements straight from the caller's arrays (one copy per object, no
+    // host staging); the DoF vectors are small and go as one copy
     std::vector<double> hd(std::max<int64_t>(dof_count, 1));
-    for (int i = 0; i < n; ++i) {
+    for (int i = 0; i < n && e == cudaSuccess; ++i) {
       const HostObjInfo& in = b->info[i];
-      if (in.n_elems) std::memcpy(hs.data() + in.src_off, objs[i].elems, in.n_elems * elem_bytes(in.geom_type));
+      if (in.n_elems)
+        e = cudaMemcpyAsync(static_cast<unsigned char*>(b->d_src) + in.src_off, objs[i].elems,
+                            in.n_elems * elem_bytes(in.geom_type), cudaMemcpyHostToDevice, s);
       std::memcpy(hd.data() + in.dof_off, objs[i].dofs, in.n_dofs * sizeof(double));
     }
-    e = cudaMemcpyAsync(b->d_src, hs.data(), src_bytes, cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess) e = cudaMemcpyAsync(b->d_dofs, hd.data(), dof_count * sizeof(double), cudaMemcpyHostToDevice, s);
   }
   if (e == cudaSuccess)
