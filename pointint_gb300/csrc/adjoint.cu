@@ -97,7 +97,7 @@ struct AdjStage {
   float2 B[ADJ_DT * ADJ_LMAX];
   float4 dh[ADJ_DT], dl[ADJ_DT];
   float qd[ADJ_DT];
-  float so_hi[ADJ_DT], so_lo[ADJ_DT];
+  double so[ADJ_DT];  // dir . origin
 };
 
 __device__ __forceinline__ void stage_tile(AdjStage& st, const KGridDev& kg, const ObjDev& od, const float2* Bw_obj,
@@ -114,8 +114,7 @@ __device__ __forceinline__ void stage_tile(AdjStage& st, const KGridDev& kg, con
                  h.z * (Ms[2] * h.x + Ms[4] * h.y + Ms[5] * h.z);
     const double so = ((double)h.x + l.x) * od.origin[0] + ((double)h.y + l.y) * od.origin[1] +
                       ((double)h.z + l.z) * od.origin[2];
-    st.so_hi[tid] = (float)so;
-    st.so_lo[tid] = (float)(so - (double)(float)so);
+    st.so[tid] = so;
   }
   __syncthreads();
   for (int t = tid; t < ADJ_DT * kg.L; t += blockDim.x) {
@@ -128,7 +127,7 @@ __device__ __forceinline__ void stage_tile(AdjStage& st, const KGridDev& kg, con
       if (k.hi * st.dl[jj].w >= 1e-10f) {
         const float2 b = Bw_obj[q];
         const float s = kg.sqrtw[q] * (kg.sign ? kg.sign[q] : 1.f);
-        const cf e = cis(df_mul_un(k, df{st.so_hi[jj], st.so_lo[jj]}));  // e^{ik.o}
+        const cf e = cis_f64(((double)k.hi + (double)k.lo) * st.so[jj]);  // e^{ik.o}
         // B e^{-ik.o} scaled: (b.x + i b.y)(e.re - i e.im)
         v = make_float2(s * (b.x * e.re + b.y * e.im), s * (b.y * e.re - b.x * e.im));
       }
@@ -157,12 +156,14 @@ adj_surf_kernel(KGridDev kg, BatchDev b, const AdjWork* __restrict__ work, const
   const bool valid = e < od.n_elems;
   const bool disk = od.type == PI_GEOM_DISK;
   for (int r = threadIdx.x; r < kg.L; r += blockDim.x) km[r] = kg.kmag[r];
-  float4 q0 = make_float4(0.f, 0.f, 0.f, 0.f), q1 = q0;
+  float4 q0 = make_float4(0.f, 0.f, 0.f, 0.f), q1 = q0, ql = q0;
   if (valid) {
     q0 = b.surf_pool[2 * (od.elem_off + e)];
     q1 = b.surf_pool[2 * (od.elem_off + e) + 1];
+    ql = b.surf_lo[od.elem_off + e];
   }
   const float3 c = make_float3(q0.x, q0.y, q0.z), nn = make_float3(q1.x, q1.y, q1.z);
+  const float3 cl = make_float3(ql.x, ql.y, ql.z);  // centre low word
   const float p0 = q0.w, p1 = q1.w;
   kf gc[3], gn[3], gm[6];
   const float2* Bw_obj = Bw + (int64_t)wk.obj * kg.Q;
@@ -175,7 +176,7 @@ adj_surf_kernel(KGridDev kg, BatchDev b, const AdjWork* __restrict__ work, const
       const float4 h = st.dh[jj], l = st.dl[jj];
       const float3 dh = make_float3(h.x, h.y, h.z), dl = make_float3(l.x, l.y, l.z);
       const float inv_norm = h.w;
-      const df sc = cdot(dh, dl, c);
+      const df sc = cdot2(dh, dl, c, cl);
       const float sn = dh.x * nn.x + dh.y * nn.y + dh.z * nn.z;
       const float perp = fmaxf(st.qd[jj] - sn * sn, 0.f);
       const float rr = p0 * sqrt_fast(perp);
@@ -228,12 +229,14 @@ adj_tri_kernel(KGridDev kg, BatchDev b, const AdjWork* __restrict__ work, const 
   const int e = wk.first + threadIdx.x;
   const bool valid = e < od.n_elems;
   for (int r = threadIdx.x; r < kg.L; r += blockDim.x) km[r] = kg.kmag[r];
-  float4 q0 = make_float4(0.f, 0.f, 0.f, 0.f), q1 = q0, q2 = q0;
+  float4 q0 = make_float4(0.f, 0.f, 0.f, 0.f), q1 = q0, q2 = q0, ql = q0;
   if (valid) {
     q0 = b.tri_pool[3 * (od.elem_off + e)];
     q1 = b.tri_pool[3 * (od.elem_off + e) + 1];
     q2 = b.tri_pool[3 * (od.elem_off + e) + 2];
+    ql = b.tri_lo[od.elem_off + e];
   }
+  const float3 ml = make_float3(ql.x, ql.y, ql.z);  // centroid low word
   const float3 m = make_float3(q0.x, q0.y, q0.z), e1 = make_float3(q1.x, q1.y, q1.z),
                e2 = make_float3(q2.x, q2.y, q2.z), S = make_float3(q0.w, q1.w, q2.w);
   kf g[9];
@@ -247,7 +250,7 @@ adj_tri_kernel(KGridDev kg, BatchDev b, const AdjWork* __restrict__ work, const 
       const float4 h = st.dh[jj], l = st.dl[jj];
       const float3 dh = make_float3(h.x, h.y, h.z), dl = make_float3(l.x, l.y, l.z);
       const float inv_norm = h.w;
-      const df sm = cdot(dh, dl, m), d1 = cdot(dh, dl, e1), d2 = cdot(dh, dl, e2);
+      const df sm = cdot2(dh, dl, m, ml), d1 = cdot(dh, dl, e1), d2 = cdot(dh, dl, e2);
       const df sa = df_add(sm, df_div3(df_add(d1, d2)) * -1.0f);
       const df sb = df_add(sa, d1), sc = df_add(sa, d2);
       const float sp = fmaxf(fmaxf(fabsf(d1.hi), fabsf(d2.hi)), fabsf(d2.hi - d1.hi));

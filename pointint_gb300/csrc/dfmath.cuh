@@ -92,6 +92,16 @@ __device__ __forceinline__ df cdot_un(float3 dh, float3 dl, float3 x) {
   return {t.hi, s.lo + t.lo + p0.lo + p1.lo + p2.lo + (dl.x * x.x + dl.y * x.y + dl.z * x.z)};
 }
 
+// cdot_un with a double-float x = xh + xl: (dh + dl) . (xh + xl), the dl . xl
+// term (~2^-48 relative) dropped, no final renormalisation.
+__device__ __forceinline__ df cdot2_un(float3 dh, float3 dl, float3 xh, float3 xl) {
+  df p0 = two_prod(dh.x, xh.x), p1 = two_prod(dh.y, xh.y), p2 = two_prod(dh.z, xh.z);
+  df s = two_sum(p0.hi, p1.hi);
+  df t = two_sum(s.hi, p2.hi);
+  return {t.hi, s.lo + t.lo + p0.lo + p1.lo + p2.lo + (dl.x * xh.x + dl.y * xh.y + dl.z * xh.z) +
+                    (dh.x * xl.x + dh.y * xl.y + dh.z * xl.z)};
+}
+
 // (dh + dl) . (xh + xl) in double-float; the dl . xl term (~2^-48 relative)
 // is dropped.
 __device__ __forceinline__ df cdot2(float3 dh, float3 dl, float3 xh, float3 xl) {
@@ -172,6 +182,19 @@ __device__ __forceinline__ cf cis(df x) {
   r = fmaf(-n, PI_PIO2_B, r);
   r += x.lo;
   return cis_quadrant(r, q);
+}
+
+// e^{i x} for an FP64 phase of any size FP64 holds, such as the origin phase
+// e^{i k.o} of an object far from the frame's origin (cis above wants
+// |x| < ~1e5): Cody-Waite reduction by pi/2 in FP64, pi/2 = A + B with
+// A = 1.5707963267948966, B = 6.123233995736766e-17 (|pi/2 - A - B| < 2e-33),
+// then cis_quadrant.  A handful of FP64 operations, so it is used once per
+// output, not in element loops.
+__device__ __forceinline__ cf cis_f64(double x) {
+  const double n = rint(x * 0.6366197723675814);
+  double r = fma(-n, 1.5707963267948966, x);
+  r = fma(-n, 6.123233995736766e-17, r);
+  return cis_quadrant((float)r, (int)(long long)n);
 }
 
 // e^{2 pi i t} for a phase given in turns, |t| < 2^20: the nearest quarter

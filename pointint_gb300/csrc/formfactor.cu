@@ -108,7 +108,7 @@ __global__ void prepare_origin_kernel(const PrepObj* objs, ObjDev* out, int only
 
 // grid (x: element blocks, y: object).  Writes the FP32 local-frame pools.
 __global__ void prepare_elems_kernel(const PrepObj* objs, const ObjDev* od, float4* tri_pool, float4* surf_pool,
-                                     int only) {
+                                     float4* tri_lo, float4* surf_lo, int only) {
   const int oi = only >= 0 ? only : blockIdx.y;
   const PrepObj o = objs[oi];
   const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -135,13 +135,20 @@ __global__ void prepare_elems_kernel(const PrepObj* objs, const ObjDev* od, floa
     float4* dst = tri_pool + 3 * (o.pool_off + e);
     if (!ok) {  // unset vertex ids contribute nothing (triangle_mesh_dof.cpp:44-45)
       dst[0] = make_float4(0.f, 0.f, 0.f, 0.f); dst[1] = dst[0]; dst[2] = dst[0];
+      tri_lo[o.pool_off + e] = dst[0];
       return;
     }
     double S[3] = {0.5 * (e1[1] * e2[2] - e1[2] * e2[1]), 0.5 * (e1[2] * e2[0] - e1[0] * e2[2]),
                    0.5 * (e1[0] * e2[1] - e1[1] * e2[0])};
-    // centroid m = a + (e1 + e2)/3 relative to the object origin
-    dst[0] = make_float4((float)(a[0] + (e1[0] + e2[0]) / 3.0 - org[0]), (float)(a[1] + (e1[1] + e2[1]) / 3.0 - org[1]),
-                         (float)(a[2] + (e1[2] + e2[2]) / 3.0 - org[2]), (float)S[0]);
+    // centroid m = a + (e1 + e2)/3 relative to the object origin, FP32 hi + lo
+    float mh[3], ml[3];
+    for (int c = 0; c < 3; ++c) {
+      const double m = a[c] + (e1[c] + e2[c]) / 3.0 - org[c];
+      mh[c] = (float)m;
+      ml[c] = (float)(m - (double)mh[c]);
+    }
+    dst[0] = make_float4(mh[0], mh[1], mh[2], (float)S[0]);
+    tri_lo[o.pool_off + e] = make_float4(ml[0], ml[1], ml[2], 0.f);
     dst[1] = make_float4((float)e1[0], (float)e1[1], (float)e1[2], (float)S[1]);
     dst[2] = make_float4((float)e2[0], (float)e2[1], (float)e2[2], (float)S[2]);
   } else {
@@ -150,7 +157,14 @@ __global__ void prepare_elems_kernel(const PrepObj* objs, const ObjDev* od, floa
     affine_apply(o.dofs, s.c, c, true);
     affine_apply(o.dofs, s.n, n, false);  // n' = A n so that k'.n = k.(A n) with k' = A^T k
     float4* dst = surf_pool + 2 * (o.pool_off + e);
-    dst[0] = make_float4((float)(c[0] - org[0]), (float)(c[1] - org[1]), (float)(c[2] - org[2]), (float)s.p0);
+    float ch[3], cl[3];
+    for (int a = 0; a < 3; ++a) {
+      const double r = c[a] - org[a];
+      ch[a] = (float)r;
+      cl[a] = (float)(r - (double)ch[a]);
+    }
+    dst[0] = make_float4(ch[0], ch[1], ch[2], (float)s.p0);
+    surf_lo[o.pool_off + e] = make_float4(cl[0], cl[1], cl[2], 0.f);
     dst[1] = make_float4((float)n[0], (float)n[1], (float)n[2], (float)s.p1);
   }
 }
@@ -267,15 +281,19 @@ ff_kernel(KGridDev kg, BatchDev b, float2* __restrict__ J, int scale_sqrt_w, con
   Acc<R> acc;
   acc.init(run_sm);
 
-  __shared__ float4 tile[3 * FF_TILE];
+  // tile[0, 3 FF_TILE): the elements' pool entries; tile[3 FF_TILE + e]: the
+  // low word of element e's centroid (centre).
+  __shared__ float4 tile[4 * FF_TILE];
   const int n = od.n_elems;
 
   if (od.type == PI_GEOM_TRIANGLE) {
     const float4* src = b.tri_pool + 3 * od.elem_off;
+    const float4* lo = b.tri_lo + od.elem_off;
     for (int base = 0; base < n; base += FF_TILE) {
       const int cnt = min(FF_TILE, n - base);
       __syncthreads();
       for (int t = threadIdx.x; t < 3 * cnt; t += FF_THREADS) tile[t] = src[3 * (int64_t)base + t];
+      for (int t = threadIdx.x; t < cnt; t += FF_THREADS) tile[3 * FF_TILE + t] = lo[base + t];
       __syncthreads();
       if (active) {
         // chunks of FF_CHUNK elements (tiles hold a multiple of FF_CHUNK)
@@ -288,7 +306,8 @@ ff_kernel(KGridDev kg, BatchDev b, float2* __restrict__ J, int scale_sqrt_w, con
           const float3 e2 = make_float3(q2.x, q2.y, q2.z);
           // -2 (khat . S): gamma of the reference times the -2 of Phi = -2 e[..]
           const float g = -2.0f * (dh.x * q0.w + dh.y * q1.w + dh.z * q2.w) * inv_norm;
-          const df sm = cdot_un(dh, dl, m);
+          const float4 ml = tile[3 * FF_TILE + e];
+          const df sm = cdot2_un(dh, dl, m, make_float3(ml.x, ml.y, ml.z));
           const float s1 = fmaf(dh.x, e1.x, fmaf(dh.y, e1.y, dh.z * e1.z));
           const float s2 = fmaf(dh.x, e2.x, fmaf(dh.y, e2.y, dh.z * e2.z));
           const float sp = fmaxf(fmaxf(fabsf(s1), fabsf(s2)), fabsf(s2 - s1));
@@ -322,6 +341,7 @@ ff_kernel(KGridDev kg, BatchDev b, float2* __restrict__ J, int scale_sqrt_w, con
     }
   } else {
     const float4* src = b.surf_pool + 2 * od.elem_off;
+    const float4* lo = b.surf_lo + od.elem_off;
     const bool disk = od.type == PI_GEOM_DISK;
     // qd = dir^T (A A^T) dir, so |k'|^2 = kmag^2 qd
     const float* Ms = od.Msym;
@@ -332,13 +352,15 @@ ff_kernel(KGridDev kg, BatchDev b, float2* __restrict__ J, int scale_sqrt_w, con
       const int cnt = min(FF_TILE, n - base);
       __syncthreads();
       for (int t = threadIdx.x; t < 2 * cnt; t += FF_THREADS) tile[t] = src[2 * (int64_t)base + t];
+      for (int t = threadIdx.x; t < cnt; t += FF_THREADS) tile[3 * FF_TILE + t] = lo[base + t];
       __syncthreads();
       if (active) {
         for (int e0 = 0; e0 < cnt; e0 += FF_CHUNK) {
         const int e1 = min(e0 + FF_CHUNK, cnt);
         for (int e = e0; e < e1; ++e) {
           const float4 q0 = tile[2 * e], q1 = tile[2 * e + 1];
-          const df sc = cdot_un(dh, dl, make_float3(q0.x, q0.y, q0.z));
+          const float4 cl = tile[3 * FF_TILE + e];
+          const df sc = cdot2_un(dh, dl, make_float3(q0.x, q0.y, q0.z), make_float3(cl.x, cl.y, cl.z));
           const float sn = dh.x * q1.x + dh.y * q1.y + dh.z * q1.z;  // dir . (A n)
           const float perp = fmaxf(qd - sn * sn, 0.f);              // |k'_perp|^2 / kmag^2
           const float amp = sn * inv_norm * q1.w;                   // area|w * (k'.n)/|k|
@@ -393,19 +415,18 @@ ff_kernel(KGridDev kg, BatchDev b, float2* __restrict__ J, int scale_sqrt_w, con
     atomicMax(reinterpret_cast<unsigned*>(ev.amax), __float_as_uint(m));
     return;
   }
-  // origin phase e^{i k.o}: dir . o formed in FP64 once per thread, then double-float.
+  // origin phase e^{i k.o}: formed and reduced in FP64 once per output, so
+  // objects far from the frame's origin keep their accuracy.
   const double dox = (double)dh.x + (double)dl.x, doy = (double)dh.y + (double)dl.y,
                doz = (double)dh.z + (double)dl.z;
   const double so_d = dox * od.origin[0] + doy * od.origin[1] + doz * od.origin[2];
-  const float so_h = (float)so_d;
-  const df so = df{so_h, (float)(so_d - (double)so_h)};
   const int64_t Jrow = (int64_t)oi * kg.Q;
 #pragma unroll
   for (int i = 0; i < R; ++i) {
     const int r = rb + nrb * i;
     if (r < kg.L) {
       const int64_t q = (int64_t)r * kg.M + j;
-      cf v = cmul(cis(df_mul(df{kw[i].x, kw[i].y}, so)), cf{acc.sre(i), acc.sim(i)});
+      cf v = cmul(cis_f64(((double)kw[i].x + (double)kw[i].y) * so_d), cf{acc.sre(i), acc.sim(i)});
       if (kw[i].x * dnorm < 1e-10f) v = cf{0.f, 0.f};  // A(0) = 0 (affine_dof.cpp:64-65)
       if (scale_sqrt_w) { const float s = kg.sqrtw[q]; v.re *= s; v.im *= s; }
       J[Jrow + q] = make_float2(v.re, v.im);
@@ -443,7 +464,8 @@ int launch_prepare(pi_batch_impl* b, int only_index, cudaStream_t s) {
   PI_LAUNCHED("prepare_origin_kernel");
   if (max_elems > 0) {
     dim3 grid((unsigned)((max_elems + 255) / 256), (unsigned)nobj_launch);
-    prepare_elems_kernel<<<grid, 256, 0, s>>>(d, b->d_objs, b->d_tri_pool, b->d_surf_pool, only_index);
+    prepare_elems_kernel<<<grid, 256, 0, s>>>(d, b->d_objs, b->d_tri_pool, b->d_surf_pool, b->d_tri_lo,
+                                              b->d_surf_lo, only_index);
     PI_LAUNCHED("prepare_elems_kernel");
   }
   // The host staging array `h` has been consumed by the copy above once the

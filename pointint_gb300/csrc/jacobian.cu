@@ -110,8 +110,7 @@ __device__ __forceinline__ JacThread jac_thread(const KGridDev& kg) {
 __device__ __forceinline__ cf jac_out_scale(const JacThread& t, const KGridDev& kg, const ObjDev& od, int64_t q) {
   const double so_d = ((double)t.dh.x + t.dl.x) * od.origin[0] + ((double)t.dh.y + t.dl.y) * od.origin[1] +
                       ((double)t.dh.z + t.dl.z) * od.origin[2];
-  const float so_h = (float)so_d;
-  const cf e = cis(df_mul(t.k, df{so_h, (float)(so_d - (double)so_h)}));
+  const cf e = cis_f64(((double)t.k.hi + (double)t.k.lo) * so_d);
   const float s = (t.k.hi * t.dnorm < 1e-10f) ? 0.f : kg.sqrtw[q];
   return cf{e.re * s, e.im * s};
 }
@@ -124,9 +123,9 @@ struct TriNode {
   float3 c[3];
 };
 
-__device__ __forceinline__ TriNode tri_node(const JacThread& t, float3 m, float3 e1, float3 e2, float3 S) {
+__device__ __forceinline__ TriNode tri_node(const JacThread& t, float3 m, float3 ml, float3 e1, float3 e2, float3 S) {
   TriNode o;
-  const df sm = cdot(t.dh, t.dl, m), d1 = cdot(t.dh, t.dl, e1), d2 = cdot(t.dh, t.dl, e2);
+  const df sm = cdot2(t.dh, t.dl, m, ml), d1 = cdot(t.dh, t.dl, e1), d2 = cdot(t.dh, t.dl, e2);
   const float sp = fmaxf(fmaxf(fabsf(d1.hi), fabsf(d2.hi)), fabsf(d2.hi - d1.hi));
   const float al = t.k.hi * d1.hi, be = t.k.hi * d2.hi;
   if (t.k.hi * sp < 2.0f) {
@@ -156,9 +155,10 @@ jac_affine_tri_kernel(KGridDev kg, BatchDev b, const JacObj* __restrict__ jobs, 
   const JacObj jo = jobs[blockIdx.y];
   const ObjDev od = b.objs[jo.obj];
   const JacThread t = jac_thread(kg);
-  __shared__ float4 tile[6 * JAC_TILE];
+  __shared__ float4 tile[7 * JAC_TILE];
   kcf A, MF[9], W[3];
   const float4* pool = b.tri_pool + 3 * od.elem_off;
+  const float4* pool_lo = b.tri_lo + od.elem_off;
   const TriSrcJ* src = reinterpret_cast<const TriSrcJ*>(jo.src);
   for (int base = 0; base < od.n_elems; base += JAC_TILE) {
     const int cnt = min(JAC_TILE, od.n_elems - base);
@@ -171,16 +171,18 @@ jac_affine_tri_kernel(KGridDev kg, BatchDev b, const JacObj* __restrict__ jobs, 
       tile[6 * e + 3] = make_float4((float)s.a[0], (float)s.a[1], (float)s.a[2], 0.f);
       tile[6 * e + 4] = make_float4((float)(s.a[0] + s.e1[0]), (float)(s.a[1] + s.e1[1]), (float)(s.a[2] + s.e1[2]), 0.f);
       tile[6 * e + 5] = make_float4((float)(s.a[0] + s.e2[0]), (float)(s.a[1] + s.e2[1]), (float)(s.a[2] + s.e2[2]), 0.f);
+      tile[6 * JAC_TILE + e] = pool_lo[base + e];  // centroid low word
     }
     __syncthreads();
     if (!t.active) continue;
     for (int e = 0; e < cnt; ++e) {
-      const float4 q0 = tile[6 * e], q1 = tile[6 * e + 1], q2 = tile[6 * e + 2];
+      const float4 q0 = tile[6 * e], q1 = tile[6 * e + 1], q2 = tile[6 * e + 2], ql = tile[6 * JAC_TILE + e];
       const float3 x0[3] = {make_float3(tile[6 * e + 3].x, tile[6 * e + 3].y, tile[6 * e + 3].z),
                             make_float3(tile[6 * e + 4].x, tile[6 * e + 4].y, tile[6 * e + 4].z),
                             make_float3(tile[6 * e + 5].x, tile[6 * e + 5].y, tile[6 * e + 5].z)};
-      const TriNode o = tri_node(t, make_float3(q0.x, q0.y, q0.z), make_float3(q1.x, q1.y, q1.z),
-                                 make_float3(q2.x, q2.y, q2.z), make_float3(q0.w, q1.w, q2.w));
+      const TriNode o = tri_node(t, make_float3(q0.x, q0.y, q0.z), make_float3(ql.x, ql.y, ql.z),
+                                 make_float3(q1.x, q1.y, q1.z), make_float3(q2.x, q2.y, q2.z),
+                                 make_float3(q0.w, q1.w, q2.w));
       A.fma_add(o.d.F, -2.0f * o.gam);
       const cf Ds[3] = {o.d.Da, o.d.Db, o.d.Dc};
 #pragma unroll
@@ -239,13 +241,14 @@ jac_affine_surf_kernel(KGridDev kg, BatchDev b, const JacObj* __restrict__ jobs,
   const ObjDev od = b.objs[jo.obj];
   const JacThread t = jac_thread(kg);
   const bool disk = od.type == PI_GEOM_DISK;
-  __shared__ float4 tile[4 * JAC_TILE];
+  __shared__ float4 tile[5 * JAC_TILE];
   const float* Ms = od.Msym;
   const float qd = t.dh.x * (Ms[0] * t.dh.x + Ms[1] * t.dh.y + Ms[2] * t.dh.z) +
                    t.dh.y * (Ms[1] * t.dh.x + Ms[3] * t.dh.y + Ms[4] * t.dh.z) +
                    t.dh.z * (Ms[2] * t.dh.x + Ms[4] * t.dh.y + Ms[5] * t.dh.z);
   kcf A, Z[3], N[3], Y;
   const float4* pool = b.surf_pool + 2 * od.elem_off;
+  const float4* pool_lo = b.surf_lo + od.elem_off;
   const SurfSrcJ* src = reinterpret_cast<const SurfSrcJ*>(jo.src);
   const float k = t.k.hi, k2 = k * k;
   for (int base = 0; base < od.n_elems; base += JAC_TILE) {
@@ -257,12 +260,14 @@ jac_affine_surf_kernel(KGridDev kg, BatchDev b, const JacObj* __restrict__ jobs,
       const SurfSrcJ& s = src[base + e];  // reference centre c0 and normal n0
       tile[4 * e + 2] = make_float4((float)s.c[0], (float)s.c[1], (float)s.c[2], 0.f);
       tile[4 * e + 3] = make_float4((float)s.n[0], (float)s.n[1], (float)s.n[2], 0.f);
+      tile[4 * JAC_TILE + e] = pool_lo[base + e];  // centre low word
     }
     __syncthreads();
     if (!t.active) continue;
     for (int e = 0; e < cnt; ++e) {
       const float4 q0 = tile[4 * e], q1 = tile[4 * e + 1], c0 = tile[4 * e + 2], n0 = tile[4 * e + 3];
-      const df sc = cdot(t.dh, t.dl, make_float3(q0.x, q0.y, q0.z));
+      const float4 cl = tile[4 * JAC_TILE + e];
+      const df sc = cdot2(t.dh, t.dl, make_float3(q0.x, q0.y, q0.z), make_float3(cl.x, cl.y, cl.z));
       const float sn = t.dh.x * q1.x + t.dh.y * q1.y + t.dh.z * q1.z;
       const float perp = fmaxf(qd - sn * sn, 0.f);
       const float amp = sn * t.inv_norm;
@@ -337,8 +342,10 @@ jac_mesh_kernel(KGridDev kg, BatchDev b, const JacObj* __restrict__ jobs, const 
       const int64_t tri = te / 3;
       const int slot = (int)(te - 3 * tri);
       const float4 q0 = b.tri_pool[3 * tri], q1 = b.tri_pool[3 * tri + 1], q2 = b.tri_pool[3 * tri + 2];
-      const TriNode o = tri_node(t, make_float3(q0.x, q0.y, q0.z), make_float3(q1.x, q1.y, q1.z),
-                                 make_float3(q2.x, q2.y, q2.z), make_float3(q0.w, q1.w, q2.w));
+      const float4 ql = b.tri_lo[tri];
+      const TriNode o = tri_node(t, make_float3(q0.x, q0.y, q0.z), make_float3(ql.x, ql.y, ql.z),
+                                 make_float3(q1.x, q1.y, q1.z), make_float3(q2.x, q2.y, q2.z),
+                                 make_float3(q0.w, q1.w, q2.w));
       const cf D = slot == 0 ? o.d.Da : (slot == 1 ? o.d.Db : o.d.Dc);
       const float3 cs = o.c[slot];
 #pragma unroll

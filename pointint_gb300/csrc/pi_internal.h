@@ -65,12 +65,17 @@ struct ObjDev {
 // Pools in the kernels' layout, object-local frame, FP32:
 //   triangles: 3 x float4 per element  (m.xyz, S.x) (e1.xyz, S.y) (e2.xyz, S.z), m the centroid
 //   disks/Gaussians: 2 x float4        (c.xyz, rho|sigma) (n'.xyz, area|w)
+// plus one float4 per element in tri_lo / surf_lo: the FP32 remainder of the
+// centroid (centre) m - (float)m, so that the phase k.m keeps ~48 bits at
+// k |m| of thousands of radians.
 struct BatchDev {
   int n_obj;
   const ObjDev* objs;
   const int32_t* order;      // CTA y-index -> object (largest first)
   const float4* tri_pool;
   const float4* surf_pool;
+  const float4* tri_lo;
+  const float4* surf_lo;
 };
 
 // One form-factor evaluation of the serving path: library object `obj`,
@@ -105,6 +110,8 @@ struct pi_batch_impl {
   double* d_dofs = nullptr;  // all DoF vectors
   float4* d_tri_pool = nullptr;
   float4* d_surf_pool = nullptr;
+  float4* d_tri_lo = nullptr;
+  float4* d_surf_lo = nullptr;
   ObjDev* d_objs = nullptr;
   int32_t* d_order = nullptr;
   // TriangleMeshDoF vertex adjacency (CSR over every mesh object's vertices):
@@ -117,6 +124,7 @@ struct pi_batch_impl {
   BatchDev dev() const {
     BatchDev b;
     b.n_obj = n_obj; b.objs = d_objs; b.order = d_order; b.tri_pool = d_tri_pool; b.surf_pool = d_surf_pool;
+    b.tri_lo = d_tri_lo; b.surf_lo = d_surf_lo;
     return b;
   }
 };
