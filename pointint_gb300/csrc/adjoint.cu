@@ -96,7 +96,7 @@ struct AdjWork { int32_t obj, first; };
 struct AdjStage {
   float2 B[ADJ_DT * ADJ_LMAX];
   float4 dh[ADJ_DT], dl[ADJ_DT];
-  float qd[ADJ_DT];
+  float4 va[ADJ_DT];  // v = A^T dir and qd = |v|^2 (disks/Gaussians: k' = |k| v)
   double so[ADJ_DT];  // dir . origin
 };
 
@@ -109,9 +109,10 @@ __device__ __forceinline__ void stage_tile(AdjStage& st, const KGridDev& kg, con
     if (j < kg.M) { h = kg.dir_hi[j]; l = kg.dir_lo[j]; }
     st.dh[tid] = h;
     st.dl[tid] = l;
-    const float* Ms = od.Msym;
-    st.qd[tid] = h.x * (Ms[0] * h.x + Ms[1] * h.y + Ms[2] * h.z) + h.y * (Ms[1] * h.x + Ms[3] * h.y + Ms[4] * h.z) +
-                 h.z * (Ms[2] * h.x + Ms[4] * h.y + Ms[5] * h.z);
+    const float* Am = od.A;
+    const float vx = Am[0] * h.x + Am[3] * h.y + Am[6] * h.z, vy = Am[1] * h.x + Am[4] * h.y + Am[7] * h.z,
+                vz = Am[2] * h.x + Am[5] * h.y + Am[8] * h.z;
+    st.va[tid] = make_float4(vx, vy, vz, fmaf(vx, vx, fmaf(vy, vy, vz * vz)));
     const double so = ((double)h.x + l.x) * od.origin[0] + ((double)h.y + l.y) * od.origin[1] +
                       ((double)h.z + l.z) * od.origin[2];
     st.so[tid] = so;
@@ -156,11 +157,12 @@ adj_surf_kernel(KGridDev kg, BatchDev b, const AdjWork* __restrict__ work, const
   const bool valid = e < od.n_elems;
   const bool disk = od.type == PI_GEOM_DISK;
   for (int r = threadIdx.x; r < kg.L; r += blockDim.x) km[r] = kg.kmag[r];
-  float4 q0 = make_float4(0.f, 0.f, 0.f, 0.f), q1 = q0, ql = q0;
+  float4 q0 = make_float4(0.f, 0.f, 0.f, 0.f), q1 = q0, ql = q0, nr = q0;
   if (valid) {
     q0 = b.surf_pool[2 * (od.elem_off + e)];
     q1 = b.surf_pool[2 * (od.elem_off + e) + 1];
     ql = b.surf_lo[od.elem_off + e];
+    nr = b.surf_nref[od.elem_off + e];
   }
   const float3 c = make_float3(q0.x, q0.y, q0.z), nn = make_float3(q1.x, q1.y, q1.z);
   const float3 cl = make_float3(ql.x, ql.y, ql.z);  // centre low word
@@ -178,7 +180,11 @@ adj_surf_kernel(KGridDev kg, BatchDev b, const AdjWork* __restrict__ work, const
       const float inv_norm = h.w;
       const df sc = cdot2(dh, dl, c, cl);
       const float sn = dh.x * nn.x + dh.y * nn.y + dh.z * nn.z;
-      const float perp = fmaxf(st.qd[jj] - sn * sn, 0.f);
+      // |k'_perp|^2 / |k|^2 = qd (1 - |n|^2) + |n|^2 |v x n/|n||^2 (no cancellation near the normal)
+      const float4 va = st.va[jj];
+      const float cx = fmaf(va.y, nr.z, -va.z * nr.y), cy = fmaf(va.z, nr.x, -va.x * nr.z),
+                  cz = fmaf(va.x, nr.y, -va.y * nr.x);
+      const float perp = fmaxf(fmaf(va.w, nr.w, (1.0f - nr.w) * fmaf(cx, cx, fmaf(cy, cy, cz * cz))), 0.f);
       const float rr = p0 * sqrt_fast(perp);
       const float amp = sn * inv_norm;
       float s_c = 0.f, s_n = 0.f, s_m = 0.f;

@@ -249,7 +249,7 @@ int pi_batch_create(const pi_object* objs, int n, int on_device, pi_stream strea
                    [&](int a, int c) { return b->info[a].n_elems > b->info[c].n_elems; });
   auto cleanup = [&]() {
     cudaFree(b->d_src); cudaFree(b->d_dofs); cudaFree(b->d_tri_pool); cudaFree(b->d_surf_pool);
-    cudaFree(b->d_tri_lo); cudaFree(b->d_surf_lo);
+    cudaFree(b->d_tri_lo); cudaFree(b->d_surf_lo); cudaFree(b->d_surf_nref);
     cudaFree(b->d_objs); cudaFree(b->d_order); cudaFree(b->d_vrow); cudaFree(b->d_vent); cudaFree(b->d_vmap);
   };
   cudaError_t e = cudaSuccess;
@@ -259,6 +259,7 @@ int pi_batch_create(const pi_object* objs, int n, int on_device, pi_stream strea
   if (e == cudaSuccess) e = cudaMalloc((void**)&b->d_surf_pool, std::max<size_t>(b->n_surf * 2 * sizeof(float4), 16));
   if (e == cudaSuccess) e = cudaMalloc((void**)&b->d_tri_lo, std::max<size_t>(b->n_tri * sizeof(float4), 16));
   if (e == cudaSuccess) e = cudaMalloc((void**)&b->d_surf_lo, std::max<size_t>(b->n_surf * sizeof(float4), 16));
+  if (e == cudaSuccess) e = cudaMalloc((void**)&b->d_surf_nref, std::max<size_t>(b->n_surf * sizeof(float4), 16));
   if (e == cudaSuccess) e = cudaMalloc((void**)&b->d_objs, std::max<size_t>(n * sizeof(ObjDev), 16));
   if (e == cudaSuccess) e = cudaMalloc((void**)&b->d_order, std::max<size_t>(n * sizeof(int32_t), 16));
   if (e != cudaSuccess) { cleanup(); return cuda_fail(e, "pi_batch_create allocation"); }
@@ -321,7 +322,7 @@ int pi_batch_prepare(pi_batch b, pi_stream stream) {
 int pi_batch_destroy(pi_batch b) {
   if (!b) return PI_OK;
   cudaFree(b->d_src); cudaFree(b->d_dofs); cudaFree(b->d_tri_pool); cudaFree(b->d_surf_pool);
-  cudaFree(b->d_tri_lo); cudaFree(b->d_surf_lo);
+  cudaFree(b->d_tri_lo); cudaFree(b->d_surf_lo); cudaFree(b->d_surf_nref);
   cudaFree(b->d_objs); cudaFree(b->d_order); cudaFree(b->d_vrow); cudaFree(b->d_vent); cudaFree(b->d_vmap);
   delete b;
   return PI_OK;

@@ -64,7 +64,7 @@ __device__ __forceinline__ void anchor(const PrepObj& o, int64_t e, double* y) {
 }
 
 // One CTA per object: fixed-order mean of the anchors (deterministic), plus
-// the object's A A^T for the surfel k' = A^T k rule.
+// the object's A for the surfel k' = A^T k rule.
 __global__ void prepare_origin_kernel(const PrepObj* objs, ObjDev* out, int only) {
   const int oi = only >= 0 ? only : blockIdx.x;
   const PrepObj o = objs[oi];
@@ -90,14 +90,9 @@ __global__ void prepare_origin_kernel(const PrepObj* objs, ObjDev* out, int only
     for (int c = 0; c < 3; ++c) d.origin[c] = red[c][0] * inv;
     if (o.dof_type == PI_DOF_AFFINE) {
       const double* A = o.dofs + 3;
-      double M[3][3];
-      for (int r = 0; r < 3; ++r)
-        for (int c = 0; c < 3; ++c)
-          M[r][c] = A[3 * r] * A[3 * c] + A[3 * r + 1] * A[3 * c + 1] + A[3 * r + 2] * A[3 * c + 2];
-      d.Msym[0] = (float)M[0][0]; d.Msym[1] = (float)M[0][1]; d.Msym[2] = (float)M[0][2];
-      d.Msym[3] = (float)M[1][1]; d.Msym[4] = (float)M[1][2]; d.Msym[5] = (float)M[2][2];
+      for (int i = 0; i < 9; ++i) d.A[i] = (float)A[i];
     } else {
-      d.Msym[0] = 1.f; d.Msym[1] = 0.f; d.Msym[2] = 0.f; d.Msym[3] = 1.f; d.Msym[4] = 0.f; d.Msym[5] = 1.f;
+      for (int i = 0; i < 9; ++i) d.A[i] = (i % 4 == 0) ? 1.f : 0.f;
     }
     d.type = o.geom_type;
     d.n_elems = (int32_t)o.n_elems;
@@ -108,7 +103,7 @@ __global__ void prepare_origin_kernel(const PrepObj* objs, ObjDev* out, int only
 
 // grid (x: element blocks, y: object).  Writes the FP32 local-frame pools.
 __global__ void prepare_elems_kernel(const PrepObj* objs, const ObjDev* od, float4* tri_pool, float4* surf_pool,
-                                     float4* tri_lo, float4* surf_lo, int only) {
+                                     float4* tri_lo, float4* surf_lo, float4* surf_nref, int only) {
   const int oi = only >= 0 ? only : blockIdx.y;
   const PrepObj o = objs[oi];
   const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -165,6 +160,10 @@ __global__ void prepare_elems_kernel(const PrepObj* objs, const ObjDev* od, floa
     }
     dst[0] = make_float4(ch[0], ch[1], ch[2], (float)s.p0);
     surf_lo[o.pool_off + e] = make_float4(cl[0], cl[1], cl[2], 0.f);
+    const double nn = s.n[0] * s.n[0] + s.n[1] * s.n[1] + s.n[2] * s.n[2];
+    const double in = nn > 0.0 ? 1.0 / sqrt(nn) : 0.0;
+    surf_nref[o.pool_off + e] =
+        make_float4((float)(s.n[0] * in), (float)(s.n[1] * in), (float)(s.n[2] * in), (float)(1.0 - nn));
     dst[1] = make_float4((float)n[0], (float)n[1], (float)n[2], (float)s.p1);
   }
 }
@@ -281,8 +280,9 @@ ff_kernel(KGridDev kg, BatchDev b, float2* __restrict__ J, int scale_sqrt_w, con
   Acc<R> acc;
   acc.init(run_sm);
 
-  // tile[0, 3 FF_TILE): the elements' pool entries; tile[3 FF_TILE + e]: the
-  // low word of element e's centroid (centre).
+  // tile[0, 3 FF_TILE): the elements' pool entries (surfels use the first
+  // 2 FF_TILE and put their unit normals at tile[2 FF_TILE + e]);
+  // tile[3 FF_TILE + e]: the low word of element e's centroid (centre).
   __shared__ float4 tile[4 * FF_TILE];
   const int n = od.n_elems;
 
@@ -343,29 +343,38 @@ ff_kernel(KGridDev kg, BatchDev b, float2* __restrict__ J, int scale_sqrt_w, con
     const float4* src = b.surf_pool + 2 * od.elem_off;
     const float4* lo = b.surf_lo + od.elem_off;
     const bool disk = od.type == PI_GEOM_DISK;
-    // qd = dir^T (A A^T) dir, so |k'|^2 = kmag^2 qd
-    const float* Ms = od.Msym;
-    const float qd = dh.x * (Ms[0] * dh.x + Ms[1] * dh.y + Ms[2] * dh.z) +
-                     dh.y * (Ms[1] * dh.x + Ms[3] * dh.y + Ms[4] * dh.z) +
-                     dh.z * (Ms[2] * dh.x + Ms[4] * dh.y + Ms[5] * dh.z);
+    // v = A^T dir, so k' = kmag v and |k'|^2 = kmag^2 qd
+    const float* Am = od.A;
+    const float3 v = make_float3(Am[0] * dh.x + Am[3] * dh.y + Am[6] * dh.z, Am[1] * dh.x + Am[4] * dh.y + Am[7] * dh.z,
+                                 Am[2] * dh.x + Am[5] * dh.y + Am[8] * dh.z);
+    const float qd = fmaf(v.x, v.x, fmaf(v.y, v.y, v.z * v.z));
+    const float4* nref = b.surf_nref + od.elem_off;
     for (int base = 0; base < n; base += FF_TILE) {
       const int cnt = min(FF_TILE, n - base);
       __syncthreads();
       for (int t = threadIdx.x; t < 2 * cnt; t += FF_THREADS) tile[t] = src[2 * (int64_t)base + t];
-      for (int t = threadIdx.x; t < cnt; t += FF_THREADS) tile[3 * FF_TILE + t] = lo[base + t];
+      for (int t = threadIdx.x; t < cnt; t += FF_THREADS) {
+        tile[2 * FF_TILE + t] = nref[base + t];
+        tile[3 * FF_TILE + t] = lo[base + t];
+      }
       __syncthreads();
       if (active) {
         for (int e0 = 0; e0 < cnt; e0 += FF_CHUNK) {
         const int e1 = min(e0 + FF_CHUNK, cnt);
         for (int e = e0; e < e1; ++e) {
-          const float4 q0 = tile[2 * e], q1 = tile[2 * e + 1];
+          const float4 q0 = tile[2 * e], q1 = tile[2 * e + 1], nr = tile[2 * FF_TILE + e];
           const float4 cl = tile[3 * FF_TILE + e];
           const df sc = cdot2_un(dh, dl, make_float3(q0.x, q0.y, q0.z), make_float3(cl.x, cl.y, cl.z));
           const float sn = dh.x * q1.x + dh.y * q1.y + dh.z * q1.z;  // dir . (A n)
-          const float perp = fmaxf(qd - sn * sn, 0.f);              // |k'_perp|^2 / kmag^2
+          // |k'_perp|^2 / kmag^2 = qd (1 - |n|^2) + |n|^2 |v x n/|n||^2: its rounding
+          // shrinks with the angle to the normal, where qd - sn^2 would leave ~1e-7
+          // (a Bessel argument off by (k rho)^2 1e-7 / (2 x) rad).
+          const float cx = fmaf(v.y, nr.z, -v.z * nr.y), cy = fmaf(v.z, nr.x, -v.x * nr.z),
+                      cz = fmaf(v.x, nr.y, -v.y * nr.x);
+          const float perp = fmaf(qd, nr.w, (1.0f - nr.w) * fmaf(cx, cx, fmaf(cy, cy, cz * cz)));
           const float amp = sn * inv_norm * q1.w;                   // area|w * (k'.n)/|k|
           if (disk) {
-            const float rr = q0.w * sqrt_fast(perp);                // rho |k'_perp| / kmag
+            const float rr = q0.w * sqrt_fast(fmaxf(perp, 0.f));    // rho |k'_perp| / kmag
 #pragma unroll
             for (int i = 0; i < R; ++i) {
               const float4 kr = ld_shared_f4(kw + i);
@@ -465,7 +474,7 @@ int launch_prepare(pi_batch_impl* b, int only_index, cudaStream_t s) {
   if (max_elems > 0) {
     dim3 grid((unsigned)((max_elems + 255) / 256), (unsigned)nobj_launch);
     prepare_elems_kernel<<<grid, 256, 0, s>>>(d, b->d_objs, b->d_tri_pool, b->d_surf_pool, b->d_tri_lo,
-                                              b->d_surf_lo, only_index);
+                                              b->d_surf_lo, b->d_surf_nref, only_index);
     PI_LAUNCHED("prepare_elems_kernel");
   }
   // The host staging array `h` has been consumed by the copy above once the

@@ -241,14 +241,17 @@ jac_affine_surf_kernel(KGridDev kg, BatchDev b, const JacObj* __restrict__ jobs,
   const ObjDev od = b.objs[jo.obj];
   const JacThread t = jac_thread(kg);
   const bool disk = od.type == PI_GEOM_DISK;
-  __shared__ float4 tile[5 * JAC_TILE];
-  const float* Ms = od.Msym;
-  const float qd = t.dh.x * (Ms[0] * t.dh.x + Ms[1] * t.dh.y + Ms[2] * t.dh.z) +
-                   t.dh.y * (Ms[1] * t.dh.x + Ms[3] * t.dh.y + Ms[4] * t.dh.z) +
-                   t.dh.z * (Ms[2] * t.dh.x + Ms[4] * t.dh.y + Ms[5] * t.dh.z);
+  __shared__ float4 tile[6 * JAC_TILE];
+  // v = A^T dir (k' = |k| v), qd = |v|^2
+  const float* Af = od.A;
+  const float3 v = make_float3(Af[0] * t.dh.x + Af[3] * t.dh.y + Af[6] * t.dh.z,
+                               Af[1] * t.dh.x + Af[4] * t.dh.y + Af[7] * t.dh.z,
+                               Af[2] * t.dh.x + Af[5] * t.dh.y + Af[8] * t.dh.z);
+  const float qd = fmaf(v.x, v.x, fmaf(v.y, v.y, v.z * v.z));
   kcf A, Z[3], N[3], Y;
   const float4* pool = b.surf_pool + 2 * od.elem_off;
   const float4* pool_lo = b.surf_lo + od.elem_off;
+  const float4* pool_nref = b.surf_nref + od.elem_off;
   const SurfSrcJ* src = reinterpret_cast<const SurfSrcJ*>(jo.src);
   const float k = t.k.hi, k2 = k * k;
   for (int base = 0; base < od.n_elems; base += JAC_TILE) {
@@ -261,6 +264,7 @@ jac_affine_surf_kernel(KGridDev kg, BatchDev b, const JacObj* __restrict__ jobs,
       tile[4 * e + 2] = make_float4((float)s.c[0], (float)s.c[1], (float)s.c[2], 0.f);
       tile[4 * e + 3] = make_float4((float)s.n[0], (float)s.n[1], (float)s.n[2], 0.f);
       tile[4 * JAC_TILE + e] = pool_lo[base + e];  // centre low word
+      tile[5 * JAC_TILE + e] = pool_nref[base + e];  // (n / |n|, 1 - |n|^2)
     }
     __syncthreads();
     if (!t.active) continue;
@@ -269,7 +273,11 @@ jac_affine_surf_kernel(KGridDev kg, BatchDev b, const JacObj* __restrict__ jobs,
       const float4 cl = tile[4 * JAC_TILE + e];
       const df sc = cdot2(t.dh, t.dl, make_float3(q0.x, q0.y, q0.z), make_float3(cl.x, cl.y, cl.z));
       const float sn = t.dh.x * q1.x + t.dh.y * q1.y + t.dh.z * q1.z;
-      const float perp = fmaxf(qd - sn * sn, 0.f);
+      // |k'_perp|^2 / |k|^2 = qd (1 - |n|^2) + |n|^2 |v x n/|n||^2 (no cancellation near the normal)
+      const float4 nr = tile[5 * JAC_TILE + e];
+      const float cx = fmaf(v.y, nr.z, -v.z * nr.y), cy = fmaf(v.z, nr.x, -v.x * nr.z),
+                  cz = fmaf(v.x, nr.y, -v.y * nr.x);
+      const float perp = fmaxf(fmaf(qd, nr.w, (1.0f - nr.w) * fmaf(cx, cx, fmaf(cy, cy, cz * cz))), 0.f);
       const float amp = sn * t.inv_norm;
       const cf P = cis(df_mul_un(t.k, sc));
       float S, Sr;

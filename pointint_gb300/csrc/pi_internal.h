@@ -56,7 +56,7 @@ struct pi_kgrid_impl {
 // ---- device object batch -----------------------------------------------------
 struct ObjDev {
   double origin[3];       // local-frame origin (transformed element centroid)
-  float Msym[6];          // A A^T (xx, xy, xz, yy, yz, zz) for disks/Gaussians
+  float A[9];             // A, row-major (identity without AffineDoF): k' = A^T k
   int32_t type;           // PI_GEOM_*
   int32_t n_elems;
   int64_t elem_off;       // offset (in elements) into the pool of its type
@@ -67,7 +67,10 @@ struct ObjDev {
 //   disks/Gaussians: 2 x float4        (c.xyz, rho|sigma) (n'.xyz, area|w)
 // plus one float4 per element in tri_lo / surf_lo: the FP32 remainder of the
 // centroid (centre) m - (float)m, so that the phase k.m keeps ~48 bits at
-// k |m| of thousands of radians.
+// k |m| of thousands of radians; and for disks/Gaussians one float4 in
+// surf_nref: (n / |n|, 1 - |n|^2) of the reference-frame normal n, for
+// |k'_perp|^2 = |k'|^2 - (k'.n)^2 = |k'|^2 (1 - |n|^2) + |n|^2 |k' x n/|n||^2
+// without the cancellation of the difference form near the normal.
 struct BatchDev {
   int n_obj;
   const ObjDev* objs;
@@ -76,6 +79,7 @@ struct BatchDev {
   const float4* surf_pool;
   const float4* tri_lo;
   const float4* surf_lo;
+  const float4* surf_nref;
 };
 
 // One form-factor evaluation of the serving path: library object `obj`,
@@ -112,6 +116,7 @@ struct pi_batch_impl {
   float4* d_surf_pool = nullptr;
   float4* d_tri_lo = nullptr;
   float4* d_surf_lo = nullptr;
+  float4* d_surf_nref = nullptr;
   ObjDev* d_objs = nullptr;
   int32_t* d_order = nullptr;
   // TriangleMeshDoF vertex adjacency (CSR over every mesh object's vertices):
@@ -124,7 +129,7 @@ struct pi_batch_impl {
   BatchDev dev() const {
     BatchDev b;
     b.n_obj = n_obj; b.objs = d_objs; b.order = d_order; b.tri_pool = d_tri_pool; b.surf_pool = d_surf_pool;
-    b.tri_lo = d_tri_lo; b.surf_lo = d_surf_lo;
+    b.tri_lo = d_tri_lo; b.surf_lo = d_surf_lo; b.surf_nref = d_surf_nref;
     return b;
   }
 };

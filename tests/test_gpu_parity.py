@@ -107,6 +107,22 @@ def test_volume_matrix_matches_oracle(cuda, orc, kg29):
     assert err.max() <= VOL_TOL, (err.max(), np.unravel_index(err.argmax(), err.shape))
 
 
+@pytest.mark.parametrize("seed", [3, 11])
+def test_volume_matrix_64_radii_matches_oracle(cuda, orc, seed):
+    """The same object kinds on a 64-radius grid (k up to 1,832, where the
+    quadrature weights are largest): a mesh against a disk cloud measured
+    2.3e-5 and 1.5e-5 here while a disk's |k'_perp|^2 was formed as the
+    difference qd - (k'.n)^2, and FP32 element centroids alone leave phase
+    errors of k |m| 6e-8 rad."""
+    kg = standard_kgrid(29, 64)
+    rng = np.random.default_rng(seed)
+    objs = [shapes(k, rng) for k in KINDS]
+    V = core.volume_matrix(kg, objs).cpu().numpy()
+    R, _, _ = orc.volume_matrix(to_oracle(orc, objs), (kg.dirs, kg.kmag, kg.w))
+    err = cond_rel_err(V, R)
+    assert err.max() <= VOL_TOL, (err.max(), [KINDS[i] for i in np.unravel_index(err.argmax(), err.shape)])
+
+
 def test_far_translation_leaves_volumes_unchanged(cuda, orc):
     """Every object moved by the same far offset (|t| ~ 4,600, so origin
     phases k.o reach ~9e6 rad at the largest of 64 radii) gives the same volume
