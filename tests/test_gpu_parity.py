@@ -104,6 +104,7 @@ def test_volume_matrix_matches_oracle(cuda, orc, kg29):
     R, _, _ = orc.volume_matrix(to_oracle(orc, objs), (kg29.dirs, kg29.kmag, kg29.w))
     assert np.array_equal(V, V.T)
     err = cond_rel_err(V, R)
+    print(f"\nvolume matrix, 32 radii: max cond rel err {err.max():.3e}")
     assert err.max() <= VOL_TOL, (err.max(), np.unravel_index(err.argmax(), err.shape))
 
 
@@ -120,6 +121,7 @@ def test_volume_matrix_64_radii_matches_oracle(cuda, orc, seed):
     V = core.volume_matrix(kg, objs).cpu().numpy()
     R, _, _ = orc.volume_matrix(to_oracle(orc, objs), (kg.dirs, kg.kmag, kg.w))
     err = cond_rel_err(V, R)
+    print(f"\n64 radii, seed {seed}: max cond rel err {err.max():.3e}")
     assert err.max() <= VOL_TOL, (err.max(), [KINDS[i] for i in np.unravel_index(err.argmax(), err.shape)])
 
 
@@ -173,6 +175,7 @@ def test_pair_sweep_config_matches_oracle(cuda, orc):
     got = np.array(got)
     scale = 1e-3 * np.sqrt(diag[0] * diag[1:])
     err = np.abs(got - ref) / np.maximum(np.abs(ref), scale)
+    print(f"\npair sweep: max cond rel err {err.max():.3e}")
     assert err.max() <= VOL_TOL, err.max()
     # identical through the drop-in Python binding (identity DoFs, offsets baked into geometry)
     Vs, Fs = G.icosphere(3)
