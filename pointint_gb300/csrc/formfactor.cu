@@ -135,7 +135,13 @@ __global__ void prepare_elems_kernel(const PrepObj* objs, const ObjDev* od, floa
     }
     double S[3] = {0.5 * (e1[1] * e2[2] - e1[2] * e2[1]), 0.5 * (e1[2] * e2[0] - e1[0] * e2[2]),
                    0.5 * (e1[0] * e2[1] - e1[1] * e2[0])};
-    // centroid m = a + (e1 + e2)/3 relative to the object origin, FP32 hi + lo
+    // centroid m = a + (e1 + e2)/3 relative to the object origin, FP32 hi + lo;
+    // beside its low word the longest edge (the series-length bound k |e|max)
+    const double l1 = e1[0] * e1[0] + e1[1] * e1[1] + e1[2] * e1[2];
+    const double l2 = e2[0] * e2[0] + e2[1] * e2[1] + e2[2] * e2[2];
+    const double l3 = (e2[0] - e1[0]) * (e2[0] - e1[0]) + (e2[1] - e1[1]) * (e2[1] - e1[1]) +
+                      (e2[2] - e1[2]) * (e2[2] - e1[2]);
+    const float lmax = (float)sqrt(fmax(fmax(l1, l2), l3));
     float mh[3], ml[3];
     for (int c = 0; c < 3; ++c) {
       const double m = a[c] + (e1[c] + e2[c]) / 3.0 - org[c];
@@ -143,7 +149,7 @@ __global__ void prepare_elems_kernel(const PrepObj* objs, const ObjDev* od, floa
       ml[c] = (float)(m - (double)mh[c]);
     }
     dst[0] = make_float4(mh[0], mh[1], mh[2], (float)S[0]);
-    tri_lo[o.pool_off + e] = make_float4(ml[0], ml[1], ml[2], 0.f);
+    tri_lo[o.pool_off + e] = make_float4(ml[0], ml[1], ml[2], lmax);
     dst[1] = make_float4((float)e1[0], (float)e1[1], (float)e1[2], (float)S[1]);
     dst[2] = make_float4((float)e2[0], (float)e2[1], (float)e2[2], (float)S[2]);
   } else {
@@ -308,6 +314,7 @@ ff_kernel(KGridDev kg, BatchDev b, float2* __restrict__ J, int scale_sqrt_w, con
           const float g = -2.0f * (dh.x * q0.w + dh.y * q1.w + dh.z * q2.w) * inv_norm;
           const float4 ml = tile[3 * FF_TILE + e];
           const df sm = cdot2_un(dh, dl, m, make_float3(ml.x, ml.y, ml.z));
+          const float kl = ml.w * dnorm;  // k kl bounds k sp: the short series below k kl = 1
           const float s1 = fmaf(dh.x, e1.x, fmaf(dh.y, e1.y, dh.z * e1.z));
           const float s2 = fmaf(dh.x, e2.x, fmaf(dh.y, e2.y, dh.z * e2.z));
           const float sp = fmaxf(fmaxf(fabsf(s1), fabsf(s2)), fabsf(s2 - s1));
@@ -321,7 +328,9 @@ ff_kernel(KGridDev kg, BatchDev b, float2* __restrict__ J, int scale_sqrt_w, con
             const float k = kr.x;
             const cf P = cis(df_mul_un(df{kr.x, kr.y}, sm));  // centroid phase, double-float
             cf T;
-            if (k < kthr) {
+            if (k * kl < 1.0f) {  // the same for all lanes on a tensor grid (unit directions)
+              T = tri_series_eval_short(tp, kr.z, kr.w);
+            } else if (k < kthr) {
               T = tri_series_eval(tp, kr.z, kr.w);  // centroid Taylor series, gamma folded in
             } else {
               // Large spread: e[pa, pb, pc] = e^{i k.m} e[k da, k db, k dc].  The
