@@ -123,13 +123,20 @@ struct TriNode {
   float3 c[3];
 };
 
-__device__ __forceinline__ TriNode tri_node(const JacThread& t, float3 m, float3 ml, float3 e1, float3 e2, float3 S) {
+// ml: the centroid's low word, and in .w the longest edge (the series-length bound).
+__device__ __forceinline__ TriNode tri_node(const JacThread& t, float3 m, float4 ml, float3 e1, float3 e2, float3 S) {
   TriNode o;
-  const df sm = cdot2(t.dh, t.dl, m, ml), d1 = cdot(t.dh, t.dl, e1), d2 = cdot(t.dh, t.dl, e2);
+  const df sm = cdot2(t.dh, t.dl, m, make_float3(ml.x, ml.y, ml.z)), d1 = cdot(t.dh, t.dl, e1),
+           d2 = cdot(t.dh, t.dl, e2);
   const float sp = fmaxf(fmaxf(fabsf(d1.hi), fabsf(d2.hi)), fabsf(d2.hi - d1.hi));
   const float al = t.k.hi * d1.hi, be = t.k.hi * d2.hi;
   if (t.k.hi * sp < 2.0f) {
-    o.d = tri_series_der(cis(df_mul_un(t.k, sm)), al, be);
+    const cf P = cis(df_mul_un(t.k, sm));
+    // the lanes of a warp share the radius and the element: a uniform branch
+    if (t.k.hi * t.dnorm * ml.w < 1.0f)
+      o.d = tri_series_der<8>(P, al, be);
+    else
+      o.d = tri_series_der<12>(P, al, be);
   } else {
     const df sa = df_add(sm, df_div3(df_add(d1, d2)) * -1.0f);
     const df sb = df_add(sa, d1), sc = df_add(sa, d2);
@@ -180,9 +187,8 @@ jac_affine_tri_kernel(KGridDev kg, BatchDev b, const JacObj* __restrict__ jobs, 
       const float3 x0[3] = {make_float3(tile[6 * e + 3].x, tile[6 * e + 3].y, tile[6 * e + 3].z),
                             make_float3(tile[6 * e + 4].x, tile[6 * e + 4].y, tile[6 * e + 4].z),
                             make_float3(tile[6 * e + 5].x, tile[6 * e + 5].y, tile[6 * e + 5].z)};
-      const TriNode o = tri_node(t, make_float3(q0.x, q0.y, q0.z), make_float3(ql.x, ql.y, ql.z),
-                                 make_float3(q1.x, q1.y, q1.z), make_float3(q2.x, q2.y, q2.z),
-                                 make_float3(q0.w, q1.w, q2.w));
+      const TriNode o = tri_node(t, make_float3(q0.x, q0.y, q0.z), ql, make_float3(q1.x, q1.y, q1.z),
+                                 make_float3(q2.x, q2.y, q2.z), make_float3(q0.w, q1.w, q2.w));
       A.fma_add(o.d.F, -2.0f * o.gam);
       const cf Ds[3] = {o.d.Da, o.d.Db, o.d.Dc};
 #pragma unroll
@@ -351,9 +357,8 @@ jac_mesh_kernel(KGridDev kg, BatchDev b, const JacObj* __restrict__ jobs, const 
       const int slot = (int)(te - 3 * tri);
       const float4 q0 = b.tri_pool[3 * tri], q1 = b.tri_pool[3 * tri + 1], q2 = b.tri_pool[3 * tri + 2];
       const float4 ql = b.tri_lo[tri];
-      const TriNode o = tri_node(t, make_float3(q0.x, q0.y, q0.z), make_float3(ql.x, ql.y, ql.z),
-                                 make_float3(q1.x, q1.y, q1.z), make_float3(q2.x, q2.y, q2.z),
-                                 make_float3(q0.w, q1.w, q2.w));
+      const TriNode o = tri_node(t, make_float3(q0.x, q0.y, q0.z), ql, make_float3(q1.x, q1.y, q1.z),
+                                 make_float3(q2.x, q2.y, q2.z), make_float3(q0.w, q1.w, q2.w));
       const cf D = slot == 0 ? o.d.Da : (slot == 1 ? o.d.Db : o.d.Dc);
       const float3 cs = o.c[slot];
 #pragma unroll

@@ -25,7 +25,13 @@ struct TriDer { cf F, Da, Db, Dc; };
 
 __device__ __forceinline__ cf imul(cf a) { return {-a.im, a.re}; }  // i a
 
+// Terms up to h_MM: MM = 12 for k sp < 2; MM = 8 where k |e|max < 1 (|e|max
+// the longest edge), where the dropped terms of F, D_b, D_c stay below 1e-8 of
+// the leading ones (FP64 evaluation over icosphere and box triangles at the
+// bound).
+template <int MM>
 __device__ __forceinline__ TriDer tri_series_der(cf P, float al, float be) {
+  static_assert(MM >= 4 && MM <= 12, "tri_series_der: order out of range");
   const float da = -(al + be) * (1.0f / 3.0f);
   const float db = al + da, dc = be + da;
   const float me2 = 0.5f * (da * da + db * db + dc * dc);
@@ -33,14 +39,14 @@ __device__ __forceinline__ TriDer tri_series_der(cf P, float al, float be) {
   float h[13];
   h[0] = 1.f; h[1] = 0.f; h[2] = me2; h[3] = e3;
 #pragma unroll
-  for (int m = 4; m <= 12; ++m) h[m] = fmaf(me2, h[m - 2], e3 * h[m - 3]);
+  for (int m = 4; m <= MM; ++m) h[m] = fmaf(me2, h[m - 2], e3 * h[m - 3]);
   // i^{m+2}/(m+2)!  and  i^{m+3}/(m+3)!  split into real / imaginary parts
   const float inv_fact[16] = {1.f, 1.f, 0.5f, 1.f / 6, 1.f / 24, 1.f / 120, 1.f / 720, 1.f / 5040, 1.f / 40320,
                               1.f / 362880, 1.f / 3628800, 1.f / 39916800, 1.f / 479001600, 1.f / 6227020800.f,
                               1.f / 87178291200.f, 1.f / 1307674368000.f};
   float Fre = 0.f, Fim = 0.f;
 #pragma unroll
-  for (int m = 0; m <= 12; ++m) {
+  for (int m = 0; m <= MM; ++m) {
     const int p = (m + 2) & 3;  // i^p: 0 -> 1, 1 -> i, 2 -> -1, 3 -> -i
     const float t = h[m] * inv_fact[m + 2];
     if (p == 0) Fre += t; else if (p == 1) Fim += t; else if (p == 2) Fre -= t; else Fim -= t;
@@ -48,7 +54,7 @@ __device__ __forceinline__ TriDer tri_series_der(cf P, float al, float be) {
   float hb = 1.f, hc = 1.f;  // h^(v)_0
   float Bre = 0.f, Bim = 0.f, Cre = 0.f, Cim = 0.f;
 #pragma unroll
-  for (int m = 0; m <= 12; ++m) {
+  for (int m = 0; m <= MM; ++m) {
     if (m > 0) { hb = fmaf(db, hb, h[m]); hc = fmaf(dc, hc, h[m]); }
     const int p = (m + 3) & 3;
     const float f = inv_fact[m + 3];
