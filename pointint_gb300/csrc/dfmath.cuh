@@ -69,11 +69,6 @@ __device__ __forceinline__ df df_mul_un(df a, df b) {
   return {p, fmaf(a.hi, b.lo, fmaf(a.lo, b.hi, fmaf(a.hi, b.hi, -p)))};
 }
 
-__device__ __forceinline__ df df_scale(df a, float s) {  // a * s, s exact
-  df p = two_prod(a.hi, s);
-  return quick_two_sum(p.hi, fmaf(a.lo, s, p.lo));
-}
-
 // (dh + dl) . x in double-float, x in FP32.
 __device__ __forceinline__ df cdot(float3 dh, float3 dl, float3 x) {
   df p0 = two_prod(dh.x, x.x), p1 = two_prod(dh.y, x.y), p2 = two_prod(dh.z, x.z);
@@ -83,17 +78,9 @@ __device__ __forceinline__ df cdot(float3 dh, float3 dl, float3 x) {
   return quick_two_sum(t.hi, lo);
 }
 
-// cdot without the final renormalisation: (hi, lo) with |lo| a few ulp of
+// (dh + dl) . (xh + xl) in double-float, the dl . xl term (~2^-48 relative)
+// dropped, without the final renormalisation: (hi, lo) with |lo| a few ulp of
 // hi, enough for df_mul_un and cis, which treat the two parts separately.
-__device__ __forceinline__ df cdot_un(float3 dh, float3 dl, float3 x) {
-  df p0 = two_prod(dh.x, x.x), p1 = two_prod(dh.y, x.y), p2 = two_prod(dh.z, x.z);
-  df s = two_sum(p0.hi, p1.hi);
-  df t = two_sum(s.hi, p2.hi);
-  return {t.hi, s.lo + t.lo + p0.lo + p1.lo + p2.lo + (dl.x * x.x + dl.y * x.y + dl.z * x.z)};
-}
-
-// cdot_un with a double-float x = xh + xl: (dh + dl) . (xh + xl), the dl . xl
-// term (~2^-48 relative) dropped, no final renormalisation.
 __device__ __forceinline__ df cdot2_un(float3 dh, float3 dl, float3 xh, float3 xl) {
   df p0 = two_prod(dh.x, xh.x), p1 = two_prod(dh.y, xh.y), p2 = two_prod(dh.z, xh.z);
   df s = two_sum(p0.hi, p1.hi);
@@ -195,16 +182,6 @@ __device__ __forceinline__ cf cis_f64(double x) {
   double r = fma(-n, 1.5707963267948966, x);
   r = fma(-n, 6.123233995736766e-17, r);
   return cis_quadrant((float)r, (int)(long long)n);
-}
-
-// e^{2 pi i t} for a phase given in turns, |t| < 2^20: the nearest quarter
-// turn n/4 is removed exactly (t - n/4 needs no more bits than t), and
-// r = 2 pi (t - n/4) lies in [-pi/4, pi/4] up to rounding.
-__device__ __forceinline__ cf cis_turns(float t) {
-  float n;
-  const int q = round_fma(4.0f, t, 0.0f, &n);
-  const float r = fmaf(-0.25f, n, t) * 6.283185307179586f;
-  return cis_quadrant(r, q);
 }
 
 __device__ __forceinline__ cf cmul(cf a, cf b) { return {a.re * b.re - a.im * b.im, a.re * b.im + a.im * b.re}; }
