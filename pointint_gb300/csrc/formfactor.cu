@@ -237,7 +237,7 @@ struct Acc {
 // otherwise it indexes the batch's objects (largest first) and J is written
 // q-major with the origin phase.
 template <int R, bool SERVE>
-__global__ void __launch_bounds__(FF_THREADS, 4)
+__global__ void __launch_bounds__(FF_THREADS, 5)
 ff_kernel(KGridDev kg, BatchDev b, float2* __restrict__ J, int scale_sqrt_w, const EvalDev* __restrict__ evals) {
   const int oi = SERVE ? evals[blockIdx.y].obj : b.order[blockIdx.y];
   const ObjDev od = b.objs[oi];
