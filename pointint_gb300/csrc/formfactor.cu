@@ -7,8 +7,8 @@
 //
 //  * prepare_*: each object's elements are transformed once per DoF change by
 //    its AffineDoF / TriangleMeshDoF into an FP32 object-local frame (origin =
-//    centroid of the transformed anchors); the origin phase e^{ik.o} is applied
-//    per output in double-float.
+//    centroid of the transformed anchors), centroids (centres) as FP32 hi + lo;
+//    the origin phase e^{ik.o} is formed and reduced in FP64 per output.
 //  * ff_kernel: one CTA = one object x 4 warps; a warp owns 32 directions
 //    (one per lane) x R radial nodes of the factored k-grid, so each element's
 //    direction dot products and series coefficients are formed once and
