@@ -336,10 +336,11 @@ def run_gb300(args):
 
 
 # DRAM bytes (read + write) of one full-size ff_kernel launch: captured with
-# ncu on 32 of the 256 objects (82,112 triangles: 4.73 MB read, writes held in
-# L2 at kernel end; profiles/ff_kernel_matrix256_32objects.md) and scaled by the
-# triangle count (656,896 / 82,112): element reads grow with the elements.
-FF_TRAFFIC_BYTES_PER_LAUNCH = 4.73e6 * 656896 / 82112
+# ncu on 32 of the 256 objects (82,112 triangles: 5.69 MB read with the
+# centroid low words, writes held in L2 at kernel end;
+# profiles/ff_kernel_matrix256_32objects.md) and scaled by the triangle count
+# (656,896 / 82,112): element reads grow with the elements.
+FF_TRAFFIC_BYTES_PER_LAUNCH = 5.69e6 * 656896 / 82112
 
 
 def _pcts(ms):
