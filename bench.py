@@ -335,12 +335,14 @@ def run_gb300(args):
         dist.destroy_process_group()
 
 
-# DRAM bytes (read + write) of one full-size ff_kernel launch: captured with
-# ncu on 32 of the 256 objects (82,112 triangles: 5.69 MB read with the
-# centroid low words, writes held in L2 at kernel end;
-# profiles/ff_kernel_matrix256_32objects.md) and scaled by the triangle count
-# (656,896 / 82,112): element reads grow with the elements.
-FF_TRAFFIC_BYTES_PER_LAUNCH = 5.69e6 * 656896 / 82112
+# DRAM bytes (read + write) of one full-size ff_kernel launch.  Reads: captured
+# with ncu on 32 of the 256 objects (82,112 triangles: 5.69 MB with the
+# centroid low words; profiles/ff_kernel_matrix256_32objects.md) and scaled by
+# the triangle count (656,896 / 82,112), since element reads grow with the
+# elements.  Writes: that capture's J (19.7 MB) stayed in L2, but the full
+# J (256 x 76,928 complex64 = 157.5 MB) exceeds the 129 MB L2 and is counted
+# as written once.
+FF_TRAFFIC_BYTES_PER_LAUNCH = 5.69e6 * 656896 / 82112 + 256 * 76928 * 8
 
 
 def _pcts(ms):
