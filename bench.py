@@ -131,56 +131,68 @@ class ClockSampler:
         return out
 
 
-def cpu_baseline_matrix256(objs, kg, seconds: float, sample_offset: int = 0):
+def workload_config(meta, n_k, world):
+    """The `config` object of both legs (same keys and values for the same workload)."""
+    return {"workload": meta["workload"], "n_k": n_k, "n_objects": meta["n_objects"],
+            "n_triangles": meta["n_triangles"], "mix": meta["mix"], "seed": "rank (0 at N=1)",
+            "l2": "GPU leg: flushed (256 MB write) before every timed step", "parallelism": f"replicas x{world}"}
+
+
+def cpu_baseline_matrix256(oobjs, kgrid, seconds: float, sample_offset: int = 0):
     """FP64 oracle (the reference algorithm restated; OpenMP over all host
-    threads) on a strided subset of k-nodes of the same workload."""
+    threads) on a strided subset of k-nodes of the same workload.  oobjs are
+    oracle objects, kgrid the (dirs, kmag, w) arrays."""
     from oracle import oracle as orc
-    oobjs = [orc.Obj(o.geom.type, o.geom.elems, o.dof_type, o.dofs) for o in objs]
+    dirs, kmag, w = kgrid
     n_tri = sum(len(o.elems) for o in oobjs)
-    Q = kg.num_nodes
+    Q = len(kmag)
     # calibrate on a tiny sample, then size the stride for ~`seconds`
     stride = 4096
     t0 = time.perf_counter()
-    orc.form_factor_matrix(oobjs, kg.dirs, kg.kmag, stride=stride)
+    orc.form_factor_matrix(oobjs, dirs, kmag, stride=stride)
     dt = max(time.perf_counter() - t0, 1e-3)
     per_node = dt / len(range(0, Q, stride))
     n_nodes = max(1, int(seconds / per_node))
     stride = max(1, Q // n_nodes)
     sel = np.arange(sample_offset % stride, Q, stride)
     t0 = time.perf_counter()
-    J = orc.form_factor_matrix(oobjs, kg.dirs[sel], kg.kmag[sel])
-    orc.contract(J, kg.w[sel])
+    J = orc.form_factor_matrix(oobjs, dirs[sel], kmag[sel])
+    orc.contract(J, w[sel])
     dt = time.perf_counter() - t0
     evals = n_tri * len(sel)
     return {"value": evals / dt, "unit": UNIT, "cores": orc.max_threads(), "kind": "port",
             "sample": f"{len(sel)} of {Q} k-nodes (every {stride}th) x {n_tri} triangles, form factors + contraction, FP64",
-            "seconds": dt}
+            "seconds": dt, "evals": evals}
 
 
 def run_reference(args):
+    """The reference's CPU algorithm (FP64 oracle port: the reference's own
+    CPU path needs Eigen, TBB and libigl) on the host cores.  Inputs come from
+    oracle.workloads, byte-identical to the GPU leg's, so nothing of the
+    product package is imported or loaded here."""
     rank, world, local = dist_setup(args.gpus)
     if rank != 0:
         return
-    from pointint_gb300 import configs
-    from oracle import oracle as orc
-    kg, objs, meta = configs.matrix256(seed=0)
+    from oracle import oracle as orc, workloads
+    kg, oobjs, meta = workloads.matrix256(seed=0)
+    Q = len(kg[1])
     per_step = max(2.0, min(10.0, 150.0 / max(1, args.steps + args.warmup)))
     for w in range(args.warmup):
-        cpu_baseline_matrix256(objs, kg, per_step / 4, sample_offset=w)
-    vals, secs = [], []
+        cpu_baseline_matrix256(oobjs, kg, per_step / 4, sample_offset=w)
+    secs, evals = [], []
     for s in range(args.steps):
-        r = cpu_baseline_matrix256(objs, kg, per_step, sample_offset=s + 1)
-        vals.append(r["value"])
+        r = cpu_baseline_matrix256(oobjs, kg, per_step, sample_offset=s + 1)
         secs.append(r["seconds"])
-    v = float(statistics.median(vals))
-    n_tri = meta["n_triangles"]
-    evals_step = n_tri * kg.num_nodes
+        evals.append(r["evals"])
+    v = float(sum(evals) / sum(secs))
+    evals_step = meta["n_triangles"] * Q
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": 1e3 * evals_step / v, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
-            "config": {"workload": meta["workload"], "n_k": kg.num_nodes, "seed": 0,
-                       "note": "reference CPU path (FP64 oracle port, OpenMP) on a strided k-node sample per step; "
-                               "ms_per_step extrapolated to the full matrix"},
+            "warmup": args.warmup, "ms_per_step": 1e3 * sum(secs) / len(secs), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
+            "config": workload_config(meta, Q, world),
+            "step": ("one bounded sample of the workload: the form factors and contraction of every object at a "
+                     "strided subset of the k-nodes (ms_per_step is the measured time of that sample)"),
+            "ms_per_full_matrix_extrapolated": 1e3 * evals_step / v,
             "cpu_baseline": {"value": v, "unit": UNIT, "cores": orc.max_threads(), "kind": "port",
                              "sample": r["sample"]},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -310,9 +322,7 @@ def run_gb300(args):
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32", "data": "synthetic (seeded)",
-            "config": {"workload": meta["workload"], "n_k": Q, "n_objects": n_obj, "n_triangles": n_tri,
-                       "mix": meta["mix"], "seed": "rank", "contraction": precision,
-                       "l2": "flushed (256 MB write) before every timed step", "parallelism": f"replicas x{world}"},
+            "config": workload_config(meta, Q, world), "contraction_precision": precision,
             "vol_matrix_per_s": world * args.steps / (total_ms / 1e3),
             "contraction": contraction, "clocks": clocks, "gpu_launches": launches, "roofline": roofline}
 
@@ -324,8 +334,11 @@ def run_gb300(args):
         line["configs"] = configs_bench(args, flush)
     if rank == 0 and world == 1 and not args.no_cpu:
         try:
-            line["cpu_baseline"] = {k: v for k, v in cpu_baseline_matrix256(objs, kg, args.cpu_seconds).items()
-                                    if k != "seconds"}
+            from oracle import oracle as orc
+            oobjs = [orc.Obj(o.geom.type, o.geom.elems, o.dof_type, o.dofs) for o in objs]
+            line["cpu_baseline"] = {k: v for k, v in cpu_baseline_matrix256(oobjs, (kg.dirs, kg.kmag, kg.w),
+                                                                            args.cpu_seconds).items()
+                                    if k not in ("seconds", "evals")}
         except Exception as exc:  # the oracle must not break the GPU line
             line["cpu_baseline"] = {"value": None, "error": str(exc)}
     if rank == 0:
@@ -337,7 +350,7 @@ def run_gb300(args):
 
 # DRAM bytes (read + write) of one full-size ff_kernel launch.  Reads: captured
 # with ncu on 32 of the 256 objects (82,112 triangles: 5.69 MB with the
-# centroid low words; profiles/ff_kernel_matrix256_32objects.md) and scaled by
+# centroid low words) and scaled by
 # the triangle count (656,896 / 82,112), since element reads grow with the
 # elements.  Writes: that capture's J (19.7 MB) stayed in L2, but the full
 # J (256 x 76,928 complex64 = 157.5 MB) exceeds the 129 MB L2 and is counted

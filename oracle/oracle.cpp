@@ -450,7 +450,8 @@ int or_build_kgrid(const double* ld, const double* lw, int M, int nrad, double* 
 
 // Lebedev row (theta_deg, phi_deg) -> direction (cpp/include/quadrature/lebedev_io.hpp:37-43)
 void or_lebedev_dir(double theta_deg, double phi_deg, double* d) {
-  double th = theta_deg * PI / 180.0, ph = phi_deg * PI / 180.0;
+  // theta *= M_PI / 180.0 (lebedev_io.hpp:37-38): the factor is rounded first
+  double th = theta_deg * (PI / 180.0), ph = phi_deg * (PI / 180.0);
   d[0] = std::cos(th) * std::sin(ph); d[1] = std::sin(th) * std::sin(ph); d[2] = std::cos(ph);
 }
 
