@@ -87,17 +87,31 @@ class ObjectBatch:
 
 
 def form_factors(kgrid: KGrid, batch: ObjectBatch, scale_sqrt_w: bool = True, out: torch.Tensor | None = None,
-                 stream=None) -> torch.Tensor:
-    """J[n, q] = A_n(k_q) (times sqrt|w_q| when scale_sqrt_w), complex64 on the device."""
+                 stream=None, row_amax: torch.Tensor | None = None) -> torch.Tensor:
+    """J[n, q] = A_n(k_q) (times sqrt|w_q| when scale_sqrt_w), complex64 on the device.
+    With row_amax (float32 [n] CUDA tensor) each row's largest |Re|, |Im| is
+    written there too, for contract(..., row_amax=...)."""
     Q = kgrid.num_nodes
     n = len(batch)
     if out is None:
         out = torch.empty((n, Q), dtype=torch.complex64, device="cuda")
     if out.shape != (n, Q) or out.dtype != torch.complex64 or not out.is_contiguous():
         raise ValueError("out must be a contiguous complex64 tensor of shape (n_objects, Q)")
-    _lib.check(_lib.lib().pi_form_factors(kgrid.handle(), batch.handle, int(bool(scale_sqrt_w)),
-                                          ctypes.c_void_p(out.data_ptr()), _stream(stream)))
+    if row_amax is None:
+        _lib.check(_lib.lib().pi_form_factors(kgrid.handle(), batch.handle, int(bool(scale_sqrt_w)),
+                                              ctypes.c_void_p(out.data_ptr()), _stream(stream)))
+    else:
+        _check_amax(row_amax, n)
+        _lib.check(_lib.lib().pi_form_factors_rowmax(kgrid.handle(), batch.handle, int(bool(scale_sqrt_w)),
+                                                     ctypes.c_void_p(out.data_ptr()),
+                                                     ctypes.c_void_p(row_amax.data_ptr()), _stream(stream)))
     return out
+
+
+def _check_amax(row_amax: torch.Tensor, n: int) -> None:
+    if not (row_amax.is_cuda and row_amax.dtype == torch.float32 and row_amax.is_contiguous()
+            and row_amax.numel() == n):
+        raise ValueError("row_amax must be a contiguous float32 CUDA tensor of n_objects entries")
 
 
 class Workspace:
@@ -122,8 +136,10 @@ def contract_workspace_size(kgrid: KGrid, n: int, precision="fp32") -> int:
 
 
 def contract(kgrid: KGrid, Jw: torch.Tensor, precision="fp32", out: torch.Tensor | None = None,
-             workspace: Workspace | None = None, stream=None) -> torch.Tensor:
-    """V = Re(J^H diag(w) J) / (8 pi^3) from the sqrt|w|-scaled J; float64 [n, n]."""
+             workspace: Workspace | None = None, stream=None, row_amax: torch.Tensor | None = None) -> torch.Tensor:
+    """V = Re(J^H diag(w) J) / (8 pi^3) from the sqrt|w|-scaled J; float64 [n, n].
+    row_amax: the rows' maxima from form_factors(..., row_amax=...), which spares
+    the FP16-split contraction a pass over J."""
     if Jw.dtype != torch.complex64 or not Jw.is_contiguous() or Jw.dim() != 2 or Jw.shape[1] != kgrid.num_nodes:
         raise ValueError("Jw must be a contiguous complex64 tensor of shape (n_objects, Q)")
     n = Jw.shape[0]
@@ -131,17 +147,22 @@ def contract(kgrid: KGrid, Jw: torch.Tensor, precision="fp32", out: torch.Tensor
     if out is None:
         out = torch.empty((n, n), dtype=torch.float64, device="cuda")
     ws = (workspace or _default_ws).get(contract_workspace_size(kgrid, n, p))
-    _lib.check(_lib.lib().pi_contract(kgrid.handle(), ctypes.c_void_p(Jw.data_ptr()), int(n), p,
-                                      ctypes.c_void_p(out.data_ptr()), ctypes.c_void_p(ws.data_ptr()),
-                                      ctypes.c_size_t(ws.numel()), _stream(stream)))
+    if row_amax is not None:
+        _check_amax(row_amax, n)
+    _lib.check(_lib.lib().pi_contract_rowmax(kgrid.handle(), ctypes.c_void_p(Jw.data_ptr()),
+                                             ctypes.c_void_p(row_amax.data_ptr()) if row_amax is not None else None,
+                                             int(n), p, ctypes.c_void_p(out.data_ptr()),
+                                             ctypes.c_void_p(ws.data_ptr()), ctypes.c_size_t(ws.numel()),
+                                             _stream(stream)))
     return out
 
 
 def volume_matrix(kgrid: KGrid, objects, precision="fp32") -> torch.Tensor:
     """Cold volume matrix: form factors + contraction (device tensors)."""
     batch = objects if isinstance(objects, ObjectBatch) else ObjectBatch(objects)
-    Jw = form_factors(kgrid, batch, True)
-    return contract(kgrid, Jw, precision)
+    amax = torch.empty(len(batch), dtype=torch.float32, device="cuda")
+    Jw = form_factors(kgrid, batch, True, row_amax=amax)
+    return contract(kgrid, Jw, precision, row_amax=amax)
 
 
 def volume_matrix_host(kgrid: KGrid, objects: list[SceneObject], precision="fp32") -> np.ndarray:
@@ -349,19 +370,23 @@ class Scene:
     def volume_matrix_of_dofs(self, dofs: torch.Tensor) -> torch.Tensor:
         return _DofVolumeFn.apply(self, dofs)
 
+    def _surfel_rows(self) -> np.ndarray:
+        """Every surfel's 64-byte record as 8 doubles (c, n, rho|sigma, area|w),
+        in object order; disks and Gaussians share the layout."""
+        return np.concatenate([o.geom.elems.view(np.float64).reshape(-1, 8) for o in self.objects])
+
     def surfel_params(self):
         """Current (c, n) of every surfel, concatenated in object order (float64 CUDA)."""
-        e = np.concatenate([o.geom.elems for o in self.objects])
-        c = torch.tensor(np.stack([e["c"][:, i] for i in range(3)], 1), device="cuda")
-        n = torch.tensor(np.stack([e["n"][:, i] for i in range(3)], 1), device="cuda")
+        e = self._surfel_rows()
+        c = torch.tensor(np.ascontiguousarray(e[:, 0:3]), device="cuda")
+        n = torch.tensor(np.ascontiguousarray(e[:, 3:6]), device="cuda")
         return c, n
 
     def set_surfels(self, c: torch.Tensor, n: torch.Tensor) -> None:
         if any(o.geom.type == _lib.GEOM_TRIANGLE for o in self.objects):
             raise TypeError("surfel parameters apply to disk / Gaussian scenes only")
         if self._packed is None:
-            e = np.concatenate([o.geom.elems for o in self.objects])
-            self._packed = torch.tensor(e.view(np.float64).reshape(-1, 8), device="cuda")
+            self._packed = torch.tensor(self._surfel_rows(), device="cuda")
         self._packed[:, 0:3] = c.detach()
         self._packed[:, 3:6] = n.detach()
         off = 0
