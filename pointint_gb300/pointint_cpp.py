@@ -29,7 +29,8 @@ __all__ = ["Geometry", "KGrid", "make_triangle_mesh", "make_point_cloud", "make_
            "create_unit_cube_mesh", "create_sphere_pointcloud", "create_sphere_gaussians", "load_lebedev",
            "build_kgrid", "compute_intersection_volume_cpu", "compute_intersection_volume_cuda",
            "compute_volume_cpu", "box_box_intersection_volume", "sphere_sphere_intersection_volume",
-           "translate_points", "compute_intersection_volume_matrix_cuda", "compute_Ak_cuda"]
+           "translate_points", "compute_intersection_volume_matrix_cuda", "compute_Ak_cuda",
+           "compute_Ak_gradient_cuda"]
 
 
 def load_lebedev(path: str):
@@ -57,10 +58,15 @@ def compute_intersection_volume_cuda(geom1: Geometry, geom2: Geometry, kgrid: KG
 
 
 def compute_intersection_volume_cpu(geom1: Geometry, geom2: Geometry, kgrid: KGrid) -> float:
-    """The reference's TBB CPU path is not part of this GPU-native build: every
-    volume here is computed by the CUDA kernels.  (The FP64 CPU restatement of
-    the reference lives in the test oracle, which products must not call.)"""
-    raise NotImplementedError("pointint_gb300 has no CPU compute path; use compute_intersection_volume_cuda")
+    """Intersection volume of two geometries (identity AffineDoF), under the
+    name of the reference's CPU binding (bindings.cpp:63-69).
+
+    This build has no CPU compute path: the value comes from the same CUDA
+    kernels as compute_intersection_volume_cuda, with the same arguments and
+    result (FP32 form factors and contraction, 1e-5 relative to the FP64
+    algorithm).  Callers that used it to cross-check the GPU get the GPU
+    value twice; the FP64 cross-check lives in the test oracle."""
+    return compute_intersection_volume_cuda(geom1, geom2, kgrid)
 
 
 def compute_volume_cpu(geom: Geometry) -> float:
@@ -80,6 +86,18 @@ def compute_intersection_volume_matrix_cuda(geometries, kgrid: KGrid, block_size
         d = IDENTITY_AFFINE.copy() if dofs is None else dofs[i]
         objs.append(SceneObject(g, dt, d))
     return volume_matrix_host(kgrid, objs, precision)
+
+
+def compute_Ak_gradient_cuda(geom: Geometry, k, dof_type: int = DOF_AFFINE, dofs=None) -> np.ndarray:
+    """dA(k)/dtheta at one k-vector, complex128 of length n_dofs (reference
+    compute_intersection_volume.hpp:129-135): 12 AffineDoF entries [t, A
+    row-major] or 3V vertex coordinates; zeros at |k| < 1e-10."""
+    obj = SceneObject(geom, dof_type, IDENTITY_AFFINE.copy() if dofs is None else dofs)
+    c = obj.as_c()
+    kv = np.ascontiguousarray(k, dtype=np.float64).reshape(3)
+    out = np.zeros(2 * len(obj.dofs))
+    _lib.check(_lib.lib().pi_compute_Ak_gradient_single(ctypes.byref(c), kv.ctypes.data, out.ctypes.data))
+    return out.view(np.complex128).copy()
 
 
 def compute_Ak_cuda(geom: Geometry, k, dof_type: int = DOF_AFFINE, dofs=None) -> complex:
