@@ -57,10 +57,51 @@ def test_static_contraction_matches_workspace_entry_point(cuda, negative_weights
         assert err <= 1e-12, (call, err)  # same kernels, same split plan: identical sums
 
 
+def _cond_err(V, R):
+    d = torch.sqrt(torch.outer(torch.diagonal(R), torch.diagonal(R)).abs())
+    return ((V - R).abs() / torch.maximum(R.abs(), 1e-3 * d)).max().item()
+
+
+@pytest.mark.parametrize("n", [1500, 1920])
+def test_static_contraction_near_its_size_limit(cuda, n):
+    """1,920 objects (15 tiles of 128) is the largest count the 8 MiB array
+    holds: the plan lowers the K split to fit, so the counts below it (1,500
+    among them) all run."""
+    Q = 2000
+    g = torch.Generator(device="cuda").manual_seed(n)
+    Jw = torch.randn((n, Q), dtype=torch.complex64, device="cuda", generator=g)
+    kg = KGrid(np.tile([[0.0, 0.0, 1.0]], (Q, 1)), np.linspace(0.1, 5.0, Q), np.ones(Q))
+    ref = core.contract(kg, Jw, "fp32")
+    for call in range(2):
+        V = torch.full((n, n), float("nan"), dtype=torch.float64, device="cuda")
+        _lib.check(_static(Jw, Q, n, None, V))
+        torch.cuda.synchronize()
+        assert torch.isfinite(V).all(), call
+        err = _cond_err(V, ref)
+        assert err <= 1e-5, (n, call, err)  # the FP32 contraction tolerance
+
+
+def test_static_contraction_reads_8_byte_aligned_rows(cuda):
+    """A complex64 view offset by one node is only 8-byte aligned: the rows are
+    read element-wise, with the same sums as an aligned copy."""
+    n, Q = 70, 1202
+    g = torch.Generator(device="cuda").manual_seed(5)
+    flat = torch.randn(n * Q + 1, dtype=torch.complex64, device="cuda", generator=g)
+    Jw = flat[1:].view(n, Q)
+    assert Jw.data_ptr() % 16 == 8
+    V = torch.full((n, n), float("nan"), dtype=torch.float64, device="cuda")
+    _lib.check(_static(Jw, Q, n, None, V))
+    kg = KGrid(np.tile([[0.0, 0.0, 1.0]], (Q, 1)), np.linspace(0.1, 5.0, Q), np.ones(Q))
+    ref = core.contract(kg, Jw.contiguous().clone(), "fp32")
+    torch.cuda.synchronize()
+    assert _cond_err(V, ref) <= 1e-12
+
+
 def test_static_contraction_rejects_oversized_problems(cuda):
     kg = standard_kgrid(3, 4)
     Jw = torch.zeros((4, kg.num_nodes), dtype=torch.complex64, device="cuda")
     V = torch.zeros((4, 4), dtype=torch.float64, device="cuda")
-    rc = _static(Jw, kg.num_nodes, 4000, None, V)  # rejected before any launch
-    assert rc == 6  # PI_ERR_WORKSPACE_TOO_SMALL
-    assert b"8388608-byte" in _lib.lib().pi_last_error()
+    for n in (1921, 4000):  # rejected before any launch: 16 tiles of 128 need 136 partial tiles > 128
+        rc = _static(Jw, kg.num_nodes, n, None, V)
+        assert rc == 6  # PI_ERR_WORKSPACE_TOO_SMALL
+        assert b"8388608-byte" in _lib.lib().pi_last_error()
