@@ -184,6 +184,57 @@ __device__ __forceinline__ cf cis_f64(double x) {
   return cis_quadrant((float)r, (int)(long long)n);
 }
 
+// ---------------------------------------------------------------------------
+// Table phasors.  A phase given in units of 1/256 turn, y = 256 x / (2 pi),
+// is split as y = n + f with n = round(y) (the 1.5 * 2^23 shift: |y| < 2^22,
+// so |x| < 1.0e5 rad) and |f| <= 1/2; then
+//   e^{i x} = tab[n mod 256] e^{i c f},  c = 2 pi / 256,
+// with tab[j] = e^{2 pi i j / 256} rounded once from FP64 (per component
+// error <= 2^-25) and, on |c f| <= pi / 256 = 0.0123, cos(c f) = 1 - (c f)^2 / 2
+// and sin(c f) = c f - (c f)^3 / 6 (truncation 9.4e-10 and 2.4e-12; Taylor
+// series, whose next terms bound the error on so short an interval).  About
+// 7e-8 per component overall, the same order as FP32 rounding of the phasor.
+#define PI_TURN256 0.024543692606170259f  // 2 pi / 256
+#define PI_TURN256_C2 0.00030119642337308832f  // c^2 / 2
+#define PI_TURN256_C3 2.4641574764489986e-06f  // c^3 / 6
+
+// e^{i c f} times tab[idx] (idx already reduced mod 256).
+// cos = 1 + cm with cm = -(c f)^2 / 2 tiny: tab (cos + i sin) is formed as
+// tab + tab cm + i tab sin, so both roundings happen at the phasor's scale.
+__device__ __forceinline__ cf cis_tab_frac(const float2* tab, int idx, float f) {
+  const float f2 = f * f;
+  const float cm = f2 * -PI_TURN256_C2;
+  const float sn = f * fmaf(f2, -PI_TURN256_C3, PI_TURN256);
+  const float2 t = tab[idx];
+  return {fmaf(t.x, cm, fmaf(-t.y, sn, t.x)), fmaf(t.y, cm, fmaf(t.x, sn, t.y))};
+}
+
+// e^{i x} with x = 2 pi (kt.hi + kt.lo) (sm.hi + sm.lo) / 256: kt is a radius
+// in units of 1/256 turn per unit length (double-float), sm a direction dot
+// product (double-float, unnormalised).  The leading product's rounding is
+// recovered by an FMA against the rounded integer, so f carries the full
+// product to ~2^-25 of a unit; the cross terms are added to it (the lo.lo
+// term, ~2^-48 relative, is dropped).
+__device__ __forceinline__ cf cis_tab_df(const float2* tab, float2 kt, df sm) {
+  const float y = kt.x * sm.hi;
+  const float t = y + PI_ROUND_SHIFT;
+  const float n = t - PI_ROUND_SHIFT;
+  float f = fmaf(kt.x, sm.hi, -n);
+  f = fmaf(kt.x, sm.lo, f);
+  f = fmaf(kt.y, sm.hi, f);
+  return cis_tab_frac(tab, __float_as_int(t) & 255, f);
+}
+
+// The same for an FP32 dot product d (kt still double-float).
+__device__ __forceinline__ cf cis_tab_f(const float2* tab, float2 kt, float d) {
+  const float y = kt.x * d;
+  const float t = y + PI_ROUND_SHIFT;
+  const float n = t - PI_ROUND_SHIFT;
+  float f = fmaf(kt.x, d, -n);
+  f = fmaf(kt.y, d, f);
+  return cis_tab_frac(tab, __float_as_int(t) & 255, f);
+}
+
 __device__ __forceinline__ cf cmul(cf a, cf b) { return {a.re * b.re - a.im * b.im, a.re * b.im + a.im * b.re}; }
 __device__ __forceinline__ cf csub(cf a, cf b) { return {a.re - b.re, a.im - b.im}; }
 __device__ __forceinline__ cf cscale(cf a, float s) { return {a.re * s, a.im * s}; }

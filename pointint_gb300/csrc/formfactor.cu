@@ -238,7 +238,8 @@ struct Acc {
 // q-major with the origin phase.
 template <int R, bool SERVE>
 __global__ void __launch_bounds__(FF_THREADS, 5)
-ff_kernel(KGridDev kg, BatchDev b, float2* __restrict__ J, int scale_sqrt_w, const EvalDev* __restrict__ evals) {
+ff_kernel(KGridDev kg, BatchDev b, float2* __restrict__ J, int scale_sqrt_w, const EvalDev* __restrict__ evals,
+          unsigned* __restrict__ row_amax) {
   const int oi = SERVE ? evals[blockIdx.y].obj : b.order[blockIdx.y];
   const ObjDev od = b.objs[oi];
   const int nrb = (kg.L + R - 1) / R;
@@ -271,16 +272,21 @@ ff_kernel(KGridDev kg, BatchDev b, float2* __restrict__ J, int scale_sqrt_w, con
     }
   }
   // radii r = rb + nrb * i: every warp sees small and large k alike.
-  // The warp's radii as (k hi, k lo, k^2, k^3), in shared memory: every lane
-  // reads the same entry (a broadcast), once per element and radius, which
-  // keeps them out of the registers the element loop needs.
+  // The warp's radii as (k 256 / 2 pi hi, lo, k^2, k^3), in shared memory:
+  // every lane reads the same entry (a broadcast), once per element and
+  // radius, which keeps them out of the registers the element loop needs.
   __shared__ float4 krad[FF_WARPS][R];
+  // e^{2 pi i j / 256}, j = 0..255: the phasor table of cis_tab_*
+  __shared__ float2 ctab[256];
+  for (int t = threadIdx.x; t < 256; t += FF_THREADS) ctab[t] = kg.cis_tab[t];
   if (lane < R) {
     const int r = rb + nrb * lane;
-    const float2 k = (item < ndt * nrb && r < kg.L) ? kg.kmag[r] : make_float2(0.f, 0.f);
-    krad[warp][lane] = make_float4(k.x, k.y, k.x * k.x, k.x * k.x * k.x);
+    const bool ok = item < ndt * nrb && r < kg.L;
+    const float2 k = ok ? kg.kmag[r] : make_float2(0.f, 0.f);
+    const float2 k2 = ok ? kg.kt256[r] : make_float2(0.f, 0.f);
+    krad[warp][lane] = make_float4(k2.x, k2.y, k.x * k.x, k.x * k.x * k.x);
   }
-  __syncwarp();
+  __syncthreads();
   const float4* kw = krad[warp];
   __shared__ float run_sm[4 * R * FF_THREADS];
   Acc<R> acc;
@@ -315,29 +321,32 @@ ff_kernel(KGridDev kg, BatchDev b, float2* __restrict__ J, int scale_sqrt_w, con
           const float4 ml = tile[3 * FF_TILE + e];
           const df sm = cdot2_un(dh, dl, m, make_float3(ml.x, ml.y, ml.z));
           const float kl = ml.w * dnorm;  // k kl bounds k sp: the short series below k kl = 1
+          const float kl2 = kl * kl;
           const float s1 = fmaf(dh.x, e1.x, fmaf(dh.y, e1.y, dh.z * e1.z));
           const float s2 = fmaf(dh.x, e2.x, fmaf(dh.y, e2.y, dh.z * e2.z));
           const float sp = fmaxf(fmaxf(fabsf(s1), fabsf(s2)), fabsf(s2 - s1));
-          const float kthr = __fdividef(2.0f, sp);  // the series for k sp < 2 (inf when sp = 0)
+          const float kthr2 = __fdividef(4.0f, sp * sp);  // the series for (k sp)^2 < 4 (inf when sp = 0)
           const TriPoly tp = tri_series_coeffs(s1, s2, g);
           // vertex phases relative to the centroid (a = m - (e1 + e2)/3, b = a + e1, c = a + e2)
           const float da = -(s1 + s2) * (1.0f / 3.0f), db = da + s1, dc = da + s2;
 #pragma unroll
           for (int i = 0; i < R; ++i) {
             const float4 kr = ld_shared_f4(kw + i);
-            const float k = kr.x;
-            const cf P = cis(df_mul_un(df{kr.x, kr.y}, sm));  // centroid phase, double-float
+            const float2 kt = make_float2(kr.x, kr.y);
+            const cf P = cis_tab_df(ctab, kt, sm);  // centroid phase
             cf T;
-            if (k * kl < 1.0f) {  // the same for all lanes on a tensor grid (unit directions)
+            if (kr.z * kl2 < 1.0f) {  // the same for all lanes on a tensor grid (unit directions)
               T = tri_series_eval_short(tp, kr.z, kr.w);
-            } else if (k < kthr) {
+            } else if (kr.z < kthr2) {
               T = tri_series_eval(tp, kr.z, kr.w);  // centroid Taylor series, gamma folded in
             } else {
               // Large spread: e[pa, pb, pc] = e^{i k.m} e[k da, k db, k dc].  The
-              // relative phases are FP32 products: their error |k d| 6e-8 rad
-              // multiplies a term of size ~1/|k d|^2 here.
-              const cf v = tri_generic(cis(df{k * da, 0.f}), cis(df{k * db, 0.f}), cis(df{k * dc, 0.f}), k * s1,
-                                       k * s2);
+              // relative phases are FP32 dot products times the double-float
+              // radius: their error |k d| 6e-8 rad multiplies a term of size
+              // ~1/|k d|^2 here.
+              const float k = kr.x * PI_TURN256;
+              const cf v = tri_generic(cis_tab_f(ctab, kt, da), cis_tab_f(ctab, kt, db), cis_tab_f(ctab, kt, dc),
+                                       k * s1, k * s2);
               T = cf{g * v.re, g * v.im};
             }
             acc.re[i] = fmaf(P.re, T.re, fmaf(-P.im, T.im, acc.re[i]));
@@ -383,13 +392,13 @@ ff_kernel(KGridDev kg, BatchDev b, float2* __restrict__ J, int scale_sqrt_w, con
           const float perp = fmaf(qd, nr.w, (1.0f - nr.w) * fmaf(cx, cx, fmaf(cy, cy, cz * cz)));
           const float amp = sn * inv_norm * q1.w;                   // area|w * (k'.n)/|k|
           if (disk) {
-            const float rr = q0.w * sqrt_fast(fmaxf(perp, 0.f));    // rho |k'_perp| / kmag
+            const float rr = q0.w * sqrt_fast(fmaxf(perp, 0.f)) * PI_TURN256;  // rho |k'_perp| / kmag, per 1/256 turn
 #pragma unroll
             for (int i = 0; i < R; ++i) {
               const float4 kr = ld_shared_f4(kw + i);
               const float x = kr.x * rr;
               const float S = (x < 1e-10f) ? 1.0f : 2.0f * j1x(x);
-              const cf P = cis(df_mul_un(df{kr.x, kr.y}, sc));
+              const cf P = cis_tab_df(ctab, make_float2(kr.x, kr.y), sc);
               const float m = S * amp;
               acc.re[i] = fmaf(m, P.re, acc.re[i]);
               acc.im[i] = fmaf(m, P.im, acc.im[i]);
@@ -400,7 +409,7 @@ ff_kernel(KGridDev kg, BatchDev b, float2* __restrict__ J, int scale_sqrt_w, con
             for (int i = 0; i < R; ++i) {
               const float4 kr = ld_shared_f4(kw + i);
               const float m = __expf(hs * kr.z) * amp;
-              const cf P = cis(df_mul_un(df{kr.x, kr.y}, sc));
+              const cf P = cis_tab_df(ctab, make_float2(kr.x, kr.y), sc);
               acc.re[i] = fmaf(m, P.re, acc.re[i]);
               acc.im[i] = fmaf(m, P.im, acc.im[i]);
             }
@@ -423,7 +432,7 @@ ff_kernel(KGridDev kg, BatchDev b, float2* __restrict__ J, int scale_sqrt_w, con
       if (r < kg.L) {
         const int64_t q = (int64_t)r * kg.M + j;
         cf v{acc.sre(i), acc.sim(i)};
-        if (kw[i].x * dnorm < 1e-10f) v = cf{0.f, 0.f};  // A(0) = 0 (affine_dof.cpp:64-65)
+        if (kw[i].x * PI_TURN256 * dnorm < 1e-10f) v = cf{0.f, 0.f};  // A(0) = 0 (affine_dof.cpp:64-65)
         const float sw = kg.sqrtw[q];
         v.re *= sw; v.im *= sw;
         ev.dst[(int64_t)j * kg.L + r] = make_float2(v.re, v.im);
@@ -439,16 +448,24 @@ ff_kernel(KGridDev kg, BatchDev b, float2* __restrict__ J, int scale_sqrt_w, con
                doz = (double)dh.z + (double)dl.z;
   const double so_d = dox * od.origin[0] + doy * od.origin[1] + doz * od.origin[2];
   const int64_t Jrow = (int64_t)oi * kg.Q;
+  float m = 0.f;
 #pragma unroll
   for (int i = 0; i < R; ++i) {
     const int r = rb + nrb * i;
     if (r < kg.L) {
       const int64_t q = (int64_t)r * kg.M + j;
-      cf v = cmul(cis_f64(((double)kw[i].x + (double)kw[i].y) * so_d), cf{acc.sre(i), acc.sim(i)});
-      if (kw[i].x * dnorm < 1e-10f) v = cf{0.f, 0.f};  // A(0) = 0 (affine_dof.cpp:64-65)
+      const double kd = ((double)kw[i].x + (double)kw[i].y) * (6.283185307179586476925 / 256.0);
+      cf v = cmul(cis_f64(kd * so_d), cf{acc.sre(i), acc.sim(i)});
+      if (kw[i].x * PI_TURN256 * dnorm < 1e-10f) v = cf{0.f, 0.f};  // A(0) = 0 (affine_dof.cpp:64-65)
       if (scale_sqrt_w) { const float s = kg.sqrtw[q]; v.re *= s; v.im *= s; }
       J[Jrow + q] = make_float2(v.re, v.im);
+      m = fmaxf(m, fmaxf(fabsf(v.re), fabsf(v.im)));
     }
+  }
+  if (row_amax) {  // the row's largest |Re|, |Im| (FP32 bits order like the non-negative floats)
+    const unsigned mask = __activemask();
+    const unsigned mb = __reduce_max_sync(mask, __float_as_uint(m));
+    if (lane == __ffs(mask) - 1) atomicMax(row_amax + oi, mb);
   }
 }
 
@@ -494,8 +511,10 @@ int launch_prepare(pi_batch_impl* b, int only_index, cudaStream_t s) {
 }
 
 int launch_form_factors(const pi_kgrid_impl* kg, const pi_batch_impl* b, int scale_sqrt_w, float2* J,
-                        cudaStream_t s) {
+                        cudaStream_t s, float* row_amax) {
   if (b->n_obj == 0) return PI_OK;
+  if (row_amax) PI_CUDA(cudaMemsetAsync(row_amax, 0, (size_t)b->n_obj * sizeof(float), s));
+  unsigned* ra = reinterpret_cast<unsigned*>(row_amax);
   const KGridDev K = kg->dev;
   const BatchDev B = b->dev();
   int R = radii_per_thread(K.L);
@@ -505,9 +524,9 @@ int launch_form_factors(const pi_kgrid_impl* kg, const pi_batch_impl* b, int sca
   dim3 grid((unsigned)((items + FF_WARPS - 1) / FF_WARPS), (unsigned)b->n_obj);
   if (grid.y > 65535) return fail(PI_ERR_UNSUPPORTED, "more than 65535 objects in one batch");
   switch (R) {
-    case 8: ff_kernel<8, false><<<grid, FF_THREADS, 0, s>>>(K, B, J, scale_sqrt_w, nullptr); break;
-    case 4: ff_kernel<4, false><<<grid, FF_THREADS, 0, s>>>(K, B, J, scale_sqrt_w, nullptr); break;
-    default: ff_kernel<1, false><<<grid, FF_THREADS, 0, s>>>(K, B, J, scale_sqrt_w, nullptr); break;
+    case 8: ff_kernel<8, false><<<grid, FF_THREADS, 0, s>>>(K, B, J, scale_sqrt_w, nullptr, ra); break;
+    case 4: ff_kernel<4, false><<<grid, FF_THREADS, 0, s>>>(K, B, J, scale_sqrt_w, nullptr, ra); break;
+    default: ff_kernel<1, false><<<grid, FF_THREADS, 0, s>>>(K, B, J, scale_sqrt_w, nullptr, ra); break;
   }
   PI_LAUNCHED("ff_kernel");
   return PI_OK;
@@ -537,7 +556,8 @@ int launch_form_factors_serve(const pi_kgrid_impl* kg, const pi_batch_impl* lib,
   BatchDev B = lib->dev();
   float2* none = nullptr;
   int scale = 1;
-  void* args[5] = {&K, &B, &none, &scale, const_cast<EvalDev**>(&evals)};
+  unsigned* no_amax = nullptr;
+  void* args[6] = {&K, &B, &none, &scale, const_cast<EvalDev**>(&evals), &no_amax};
   PI_CUDA(cudaLaunchKernel(ff_serve_fn(kg), dim3((unsigned)ff_serve_grid_x(kg), (unsigned)n_evals), dim3(FF_THREADS),
                            args, 0, s));
   count_launch();

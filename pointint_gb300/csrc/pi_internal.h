@@ -41,6 +41,8 @@ struct KGridDev {
   const float* sqrtw;     // Q: sqrt(|w_q|)
   const float* sign;      // Q: sign(w_q), or nullptr when every weight is >= 0
   const float2* kturn;    // L: kmag / 2 pi (hi, lo)
+  const float2* kt256;    // L: kmag 256 / 2 pi (hi, lo): phases in units of 1/256 turn
+  const float2* cis_tab;  // 256: e^{2 pi i j / 256} (cos, sin), rounded once from FP64
 };
 
 struct pi_kgrid_impl {
@@ -136,8 +138,10 @@ struct pi_batch_impl {
 
 // ---- launchers (formfactor.cu / contract.cu) ------------------------------------
 int launch_prepare(pi_batch_impl* b, int only_index, cudaStream_t s);
+// row_amax (optional, n_objects floats): each row's largest |Re|, |Im| of the
+// written values, for the FP16 operand scales of the split contraction.
 int launch_form_factors(const pi_kgrid_impl* kg, const pi_batch_impl* b, int scale_sqrt_w, float2* J,
-                        cudaStream_t s);
+                        cudaStream_t s, float* row_amax = nullptr);
 size_t contract_fp32_ws_bytes(int64_t Q, int n);
 int launch_contract_fp32(const pi_kgrid_impl* kg, const float2* Jw, int n, double* V, void* ws, size_t ws_bytes,
                          cudaStream_t s);

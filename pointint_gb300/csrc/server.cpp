@@ -232,7 +232,8 @@ int build_graph(Server& S, Slot& sl) {
   float2* none = nullptr;
   int one = 1;
   EvalDev* evals = reinterpret_cast<EvalDev*>(sl.d_io + S.lay.evals);
-  void* ff_args[5] = {&K, &B, &none, &one, &evals};
+  unsigned* no_amax = nullptr;  // serving rows keep their maxima through EvalDev::amax
+  void* ff_args[6] = {&K, &B, &none, &one, &evals, &no_amax};
   cudaKernelNodeParams kp{};
   kp.func = const_cast<void*>(ff_serve_fn(S.kg));
   kp.gridDim = dim3((unsigned)ff_serve_grid_x(S.kg), 1);
@@ -535,7 +536,8 @@ int launch_batch(Server& S, Slot& sl, const std::vector<cudaEvent_t>& waits) {
       float2* none = nullptr;
       int one = 1;
       EvalDev* evals = reinterpret_cast<EvalDev*>(sl.d_io + S.lay.evals);
-      void* ff_args[5] = {&K, &B, &none, &one, &evals};
+      unsigned* no_amax = nullptr;
+      void* ff_args[6] = {&K, &B, &none, &one, &evals, &no_amax};
       cudaKernelNodeParams kp{};
       kp.func = const_cast<void*>(ff_serve_fn(S.kg));
       kp.gridDim = dim3((unsigned)ff_serve_grid_x(S.kg), (unsigned)sl.n_evals);
