@@ -152,6 +152,12 @@ int pi_batch_count(pi_batch b, int* n_objects);
  * scale_sqrt_w != 0 every row q is multiplied by sqrt(|w_q|) (the contraction's
  * operand form).  d_J: device, n_objects*Q*8 bytes. */
 int pi_form_factors(pi_kgrid kg, pi_batch b, int scale_sqrt_w, void* d_J, pi_stream stream);
+/* pi_form_factors that also writes each row's largest |Re|, |Im| of the values
+ * written (d_row_amax: device, n_objects floats), which pi_contract_rowmax
+ * takes as the FP16 operand scales of PI_CONTRACT_FP16X3 instead of reading J
+ * a second time to find them.  No reference counterpart. */
+int pi_form_factors_rowmax(pi_kgrid kg, pi_batch b, int scale_sqrt_w, void* d_J, float* d_row_amax,
+                           pi_stream stream);
 
 /* ---- contraction V = Re(J^H diag(w) J)/(8 pi^3) -------------------------------- */
 /* Replaces K9 and K14 (cpp/src/compute_intersection_volume.cu:33-50;
@@ -162,6 +168,27 @@ int pi_form_factors(pi_kgrid kg, pi_batch b, int scale_sqrt_w, void* d_J, pi_str
 int pi_contract_workspace_size(pi_kgrid kg, int n_objects, int precision, size_t* bytes);
 int pi_contract(pi_kgrid kg, const void* d_Jw, int n_objects, int precision, double* d_V, void* d_ws,
                 size_t ws_bytes, pi_stream stream);
+/* pi_contract with the rows' maxima given (d_row_amax: device, n_objects
+ * floats, each row's largest |Re|, |Im| or any upper bound of it, e.g. from
+ * pi_form_factors_rowmax on the same J), used by PI_CONTRACT_FP16X3; NULL
+ * finds them with a pass over J like pi_contract.  Other precisions ignore it. */
+int pi_contract_rowmax(pi_kgrid kg, const void* d_Jw, const float* d_row_amax, int n_objects, int precision,
+                       double* d_V, void* d_ws, size_t ws_bytes, pi_stream stream);
+/* Device-side status of the last tensor-core contraction that used d_ws:
+ * synchronises `stream`, then PI_OK, or PI_ERR_TIMEOUT when one of the
+ * kernel's bounded waits (~2 s of SM clock each) ran out -- the kernel then
+ * left every loop, drained its copies and tensor-core operations, freed its
+ * tensor memory and wrote NaN to V, and the context stays usable.
+ * PI_CONTRACT_FP32 has no waits and always reports PI_OK.  No reference
+ * counterpart (the reference printed CUDA errors and returned zeros). */
+int pi_contract_error(int precision, const void* d_ws, pi_stream stream);
+
+/* Testing hook, not for production use: every later single-matrix FP16 / BF16
+ * split contraction (pi_contract) waits at most wait_cycles SM clocks per
+ * barrier (<= 0 restores the built-in ~2 s) and, when starve_chunk >= 0, the
+ * loader of its first CTA never loads that chunk, so that a wait runs out
+ * without any fault.  Process-wide; call (0, -1) to undo. */
+int pi_test_set_contract_faults(int64_t wait_cycles, int64_t starve_chunk);
 
 /* Replace the packed elements of object `index` (device pointer, same count and
  * layout) and re-transform it; used by optimisation loops that move elements. */
@@ -203,9 +230,12 @@ int pi_dof_gradients(pi_kgrid kg, pi_batch b, const void* d_Jw, const double* W,
  * Inputs and output are caller-owned device buffers: d_Jw is the
  * sqrt(|w|)-scaled J (complex64, n x Q), d_sign the Q signs of the quadrature
  * weights or NULL when all are >= 0, d_V the n x n double output (1/(8 pi^3)
- * applied).  Object counts whose partial tiles exceed 8 MiB (about 1,900
- * objects on a 152-SM GB300) return PI_ERR_WORKSPACE_TOO_SMALL.  All calls
- * share the array, so calls whose kernels overlap on the GPU race. */
+ * applied).  d_Jw needs no particular alignment (8-byte aligned complex64
+ * rows are read element-wise).  Up to 1,920 objects fit the array on any GPU
+ * (the K split is lowered to stay inside it); more return
+ * PI_ERR_WORKSPACE_TOO_SMALL.  All calls share the array, so calls whose
+ * kernels overlap on the GPU race.  The array's address is looked up once per
+ * device: do not use this entry point across a cudaDeviceReset. */
 int pi_contract_fp32_static(const void* d_Jw, int64_t Q, int n_objects, const float* d_sign, double* d_V,
                             pi_stream stream);
 
@@ -264,6 +294,18 @@ int pi_compute_Ak(const pi_object* obj, const double* dirs, const double* kmag, 
 /* compute_Ak_cuda (cpp/include/compute_intersection_volume.hpp:120-126): A at one
  * k-vector, host in and out (out = re, im). */
 int pi_compute_Ak_single(const pi_object* obj, const double* k, double* out);
+/* The registry's gradient function (CudaComputeAkGradientFunc,
+ * cpp/include/dof/cuda/dof_cuda_interface.hpp:32-40): host object and k-grid,
+ * output d_grad_out = Q x D complex doubles (double2), row-major, q-major, on the
+ * device, D = obj->n_dofs: dA(k_q)/dtheta_d with the object's position phase
+ * (affine_dof.cpp:172-322, triangle_mesh_dof.cpp:76-143).  Synchronous like the
+ * reference wrapper. */
+int pi_compute_Ak_gradient(const pi_object* obj, const double* dirs, const double* kmag, int64_t Q,
+                           double* d_grad_out, int block_size);
+/* compute_Ak_gradient_cuda (cpp/include/compute_intersection_volume.hpp:129-135):
+ * dA(k)/dtheta at one k-vector, host in and out (out = D pairs re, im; zeros
+ * at |k| < 1e-10 like the reference). */
+int pi_compute_Ak_gradient_single(const pi_object* obj, const double* k, double* out);
 
 /* ---- serving: resident form factors, rigid-transform queries ----------------
  * No reference counterpart: the reference evaluates every object's form

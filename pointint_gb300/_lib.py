@@ -106,6 +106,10 @@ SIGNATURES = {
     "pi_batch_destroy": (I32, [P]),
     "pi_batch_count": (I32, [P, ctypes.POINTER(I32)]),
     "pi_form_factors": (I32, [P, P, I32, P, P]),
+    "pi_form_factors_rowmax": (I32, [P, P, I32, P, P, P]),
+    "pi_contract_rowmax": (I32, [P, P, P, I32, I32, P, P, SZ, P]),
+    "pi_contract_error": (I32, [I32, P, P]),
+    "pi_test_set_contract_faults": (I32, [I64, I64]),
     "pi_contract_workspace_size": (I32, [P, I32, I32, ctypes.POINTER(SZ)]),
     "pi_contract": (I32, [P, P, I32, I32, P, P, SZ, P]),
     "pi_contract_fp32_static": (I32, [P, I64, I32, P, P, P]),
@@ -123,6 +127,8 @@ SIGNATURES = {
     "pi_pair_volume_host": (I32, [OBJP, OBJP, P, P, P, I64, ctypes.POINTER(D)]),
     "pi_compute_Ak": (I32, [OBJP, P, P, I64, P, I32]),
     "pi_compute_Ak_single": (I32, [OBJP, P, P]),
+    "pi_compute_Ak_gradient": (I32, [OBJP, P, P, I64, P, I32]),
+    "pi_compute_Ak_gradient_single": (I32, [OBJP, P, P]),
     "pi_server_create": (I32, [P, OBJP, I32, ctypes.POINTER(ServerConfig), PP]),
     "pi_server_submit": (I32, [P, ctypes.POINTER(Query), P, ctypes.POINTER(ctypes.c_uint64)]),
     "pi_server_poll": (I32, [P, ctypes.c_uint64, ctypes.POINTER(ctypes.c_int32)]),

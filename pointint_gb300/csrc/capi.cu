@@ -70,6 +70,16 @@ struct DevBuf {
 
 struct KGridGuard { pi_kgrid k = nullptr; ~KGridGuard() { if (k) pi_kgrid_destroy(k); } };
 
+// G [D][Q] complex64 (the DoF Jacobian's layout) -> out [Q][D] double2 (the
+// registry gradient plugin's row-major layout).
+__global__ void jacobian_to_qd_kernel(const float2* __restrict__ G, int64_t Q, int64_t D, double2* __restrict__ out) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= Q * D) return;
+  const int64_t q = t / D, d = t - q * D;
+  const float2 v = G[d * Q + q];
+  out[t] = make_double2(v.x, v.y);
+}
+
 // Vertex -> (triangle, slot) adjacency of every TriangleMeshDoF object, for
 // the deterministic per-vertex gather of the adjoint.  Device-resident
 // elements are read back once.
@@ -144,7 +154,7 @@ int pi_kgrid_create(const double* dirs, const double* kmag, const double* w, int
   const int64_t L = tensor ? Q / M : 1;
   if (!tensor) M = Q;
   std::vector<float4> dh(M), dl(M);
-  std::vector<float2> km(L), kt(L);
+  std::vector<float2> km(L), kt(L), k256(L), tab(256);
   for (int64_t j = 0; j < M; ++j) {
     double d[3];
     for (int c = 0; c < 3; ++c) d[c] = tensor ? dirs[3 * j + c] : dirs[3 * j + c] * kmag[j];
@@ -161,6 +171,13 @@ int pi_kgrid_create(const double* dirs, const double* kmag, const double* w, int
     const double u = k / (2.0 * 3.14159265358979323846);
     const float uh = (float)u;
     kt[r] = make_float2(uh, (float)(u - (double)uh));
+    const double v = u * 256.0;
+    const float vh = (float)v;
+    k256[r] = make_float2(vh, (float)(v - (double)vh));
+  }
+  for (int j = 0; j < 256; ++j) {
+    const double a = 2.0 * 3.14159265358979323846 * j / 256.0;
+    tab[j] = make_float2((float)std::cos(a), (float)std::sin(a));
   }
   std::vector<float> sw(Q), sg(Q);
   kg->w.resize(Q);
@@ -174,7 +191,8 @@ int pi_kgrid_create(const double* dirs, const double* kmag, const double* w, int
   }
   const size_t o_dh = 0, o_dl = align16(o_dh + M * sizeof(float4)), o_km = align16(o_dl + M * sizeof(float4)),
                o_sw = align16(o_km + L * sizeof(float2)), o_sg = align16(o_sw + Q * sizeof(float)),
-               o_kt = align16(o_sg + Q * sizeof(float)), total = align16(o_kt + L * sizeof(float2));
+               o_kt = align16(o_sg + Q * sizeof(float)), o_k256 = align16(o_kt + L * sizeof(float2)),
+               o_tab = align16(o_k256 + L * sizeof(float2)), total = align16(o_tab + 256 * sizeof(float2));
   std::vector<unsigned char> host(total, 0);
   std::memcpy(host.data() + o_dh, dh.data(), M * sizeof(float4));
   std::memcpy(host.data() + o_dl, dl.data(), M * sizeof(float4));
@@ -182,6 +200,8 @@ int pi_kgrid_create(const double* dirs, const double* kmag, const double* w, int
   std::memcpy(host.data() + o_sw, sw.data(), Q * sizeof(float));
   std::memcpy(host.data() + o_sg, sg.data(), Q * sizeof(float));
   std::memcpy(host.data() + o_kt, kt.data(), L * sizeof(float2));
+  std::memcpy(host.data() + o_k256, k256.data(), L * sizeof(float2));
+  std::memcpy(host.data() + o_tab, tab.data(), 256 * sizeof(float2));
   PI_CUDA(cudaMalloc(&kg->d_mem, total));
   cudaError_t e = cudaMemcpy(kg->d_mem, host.data(), total, cudaMemcpyHostToDevice);
   if (e != cudaSuccess) { cudaFree(kg->d_mem); return cuda_fail(e, "pi_kgrid_create upload"); }
@@ -194,6 +214,8 @@ int pi_kgrid_create(const double* dirs, const double* kmag, const double* w, int
   kg->dev.sqrtw = reinterpret_cast<const float*>(base + o_sw);
   kg->dev.sign = reinterpret_cast<const float*>(base + o_sg);
   kg->dev.kturn = reinterpret_cast<const float2*>(base + o_kt);
+  kg->dev.kt256 = reinterpret_cast<const float2*>(base + o_k256);
+  kg->dev.cis_tab = reinterpret_cast<const float2*>(base + o_tab);
   *out = kg.release();
   return PI_OK;
 }
@@ -339,6 +361,14 @@ int pi_form_factors(pi_kgrid kg, pi_batch b, int scale_sqrt_w, void* d_J, pi_str
   return launch_form_factors(kg, b, scale_sqrt_w, static_cast<float2*>(d_J), reinterpret_cast<cudaStream_t>(stream));
 }
 
+int pi_form_factors_rowmax(pi_kgrid kg, pi_batch b, int scale_sqrt_w, void* d_J, float* d_row_amax,
+                           pi_stream stream) {
+  if (!kg || !b || ((!d_J || !d_row_amax) && b->n_obj > 0))
+    return fail(PI_ERR_INVALID_ARGUMENT, "pi_form_factors_rowmax: bad arguments");
+  return launch_form_factors(kg, b, scale_sqrt_w, static_cast<float2*>(d_J), reinterpret_cast<cudaStream_t>(stream),
+                             d_row_amax);
+}
+
 int pi_contract_workspace_size(pi_kgrid kg, int n, int precision, size_t* bytes) {
   if (!kg || !bytes || n < 0) return fail(PI_ERR_INVALID_ARGUMENT, "pi_contract_workspace_size: bad arguments");
   if (precision == PI_CONTRACT_FP32) *bytes = contract_fp32_ws_bytes(kg->Q, n);
@@ -349,8 +379,8 @@ int pi_contract_workspace_size(pi_kgrid kg, int n, int precision, size_t* bytes)
   return PI_OK;
 }
 
-int pi_contract(pi_kgrid kg, const void* d_Jw, int n, int precision, double* d_V, void* d_ws, size_t ws_bytes,
-                pi_stream stream) {
+int pi_contract_rowmax(pi_kgrid kg, const void* d_Jw, const float* d_row_amax, int n, int precision, double* d_V,
+                       void* d_ws, size_t ws_bytes, pi_stream stream) {
   if (!kg || n < 0 || (n > 0 && (!d_Jw || !d_V))) return fail(PI_ERR_INVALID_ARGUMENT, "pi_contract: bad arguments");
   cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
   const float2* J = static_cast<const float2*>(d_Jw);
@@ -360,10 +390,40 @@ int pi_contract(pi_kgrid kg, const void* d_Jw, int n, int precision, double* d_V
       return fail(PI_ERR_UNSUPPORTED, "the tensor-core contractions need non-negative quadrature weights");
     if (precision != PI_CONTRACT_TF32X3)
       return launch_group_single(J, kg->Q, n, precision == PI_CONTRACT_FP16X3 ? GROUP_OP_F16 : GROUP_OP_BF16, d_V,
-                                 d_ws, ws_bytes, INV_8PI3, s);
+                                 d_ws, ws_bytes, INV_8PI3, s, d_row_amax);
     return launch_contract_tc(kg, J, n, 1, d_V, d_ws, ws_bytes, s);
   }
   return fail(PI_ERR_INVALID_ARGUMENT, "unknown contraction precision");
+}
+
+int pi_contract(pi_kgrid kg, const void* d_Jw, int n, int precision, double* d_V, void* d_ws, size_t ws_bytes,
+                pi_stream stream) {
+  return pi_contract_rowmax(kg, d_Jw, nullptr, n, precision, d_V, d_ws, ws_bytes, stream);
+}
+
+int pi_contract_error(int precision, const void* d_ws, pi_stream stream) {
+  if (precision == PI_CONTRACT_FP32) return PI_OK;  // no waits, no error word
+  if (precision != PI_CONTRACT_BF16X3 && precision != PI_CONTRACT_TF32X3 && precision != PI_CONTRACT_FP16X3)
+    return fail(PI_ERR_INVALID_ARGUMENT, "pi_contract_error: unknown contraction precision");
+  if (!d_ws) return fail(PI_ERR_INVALID_ARGUMENT, "pi_contract_error: null workspace");
+  cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  int code = 0;
+  PI_CUDA(cudaMemcpyAsync(&code, d_ws, sizeof(int), cudaMemcpyDeviceToHost, s));
+  PI_CUDA(cudaStreamSynchronize(s));
+  if (code == 0) return PI_OK;
+  static const char* group_roles[] = {"", "loader", "converter", "MMA issuer", "epilogue", "work-item capacity"};
+  static const char* tf32_roles[] = {"", "converter", "MMA issuer", "epilogue", "loader"};
+  const char* role = precision == PI_CONTRACT_TF32X3 ? (code >= 1 && code <= 4 ? tf32_roles[code] : "unknown role")
+                                                     : (code >= 1 && code <= 5 ? group_roles[code] : "unknown role");
+  char buf[160];
+  snprintf(buf, sizeof buf, "tensor-core contraction: a bounded wait of the %s expired (device code %d); V holds NaN",
+           role, code);
+  return fail(code == 5 ? PI_ERR_WORKSPACE_TOO_SMALL : PI_ERR_TIMEOUT, buf);
+}
+
+int pi_test_set_contract_faults(int64_t wait_cycles, int64_t starve_chunk) {
+  group_test_set_faults((long long)wait_cycles, (long long)starve_chunk);
+  return PI_OK;
 }
 
 int pi_batch_set_elements(pi_batch b, int index, const void* d_elems, pi_stream stream) {
@@ -435,13 +495,15 @@ int pi_volume_matrix_host(const pi_object* objs, int n, const double* dirs, cons
   size_t ws_bytes = 0;
   rc = pi_contract_workspace_size(kg.k, n, precision, &ws_bytes);
   if (rc) return rc;
-  DevBuf J, ws, V;
+  DevBuf J, ws, V, amax;
   if ((rc = J.alloc((size_t)n * Q * sizeof(float2), s)) || (rc = ws.alloc(ws_bytes, s)) ||
-      (rc = V.alloc((size_t)n * n * sizeof(double), s)))
+      (rc = V.alloc((size_t)n * n * sizeof(double), s)) || (rc = amax.alloc((size_t)n * sizeof(float), s)))
     return rc;
-  rc = pi_form_factors(kg.k, b.b, 1, J.p, reinterpret_cast<pi_stream>(s));
+  float* row_amax = static_cast<float*>(amax.p);
+  rc = pi_form_factors_rowmax(kg.k, b.b, 1, J.p, row_amax, reinterpret_cast<pi_stream>(s));
   if (rc) return rc;
-  rc = pi_contract(kg.k, J.p, n, precision, static_cast<double*>(V.p), ws.p, ws_bytes, reinterpret_cast<pi_stream>(s));
+  rc = pi_contract_rowmax(kg.k, J.p, row_amax, n, precision, static_cast<double*>(V.p), ws.p, ws_bytes,
+                          reinterpret_cast<pi_stream>(s));
   if (rc) return rc;
   PI_CUDA(cudaMemcpyAsync(V_out, V.p, (size_t)n * n * sizeof(double), cudaMemcpyDeviceToHost, s));
   PI_CUDA(cudaStreamSynchronize(s));
@@ -658,6 +720,51 @@ int pi_compute_Ak_single(const pi_object* obj, const double* k, double* out) {
   rc = pi_compute_Ak(obj, dir, &km, 1, static_cast<double*>(d.p), 256);
   if (rc) return rc;
   PI_CUDA(cudaMemcpy(out, d.p, 2 * sizeof(double), cudaMemcpyDeviceToHost));
+  return PI_OK;
+}
+
+int pi_compute_Ak_gradient(const pi_object* obj, const double* dirs, const double* kmag, int64_t Q,
+                           double* d_grad_out, int block_size) {
+  (void)block_size;  // kept for signature parity with the registry's gradient function
+  if (!obj || !d_grad_out || Q <= 0) return fail(PI_ERR_INVALID_ARGUMENT, "pi_compute_Ak_gradient: bad arguments");
+  cudaStream_t s = cudaStreamPerThread;
+  KGridGuard kg;
+  int rc = pi_kgrid_create(dirs, kmag, nullptr, Q, &kg.k);  // unit weights: G = dA/dtheta
+  if (rc) return rc;
+  BatchGuard b;
+  rc = pi_batch_create(obj, 1, 0, reinterpret_cast<pi_stream>(s), &b.b);
+  if (rc) return rc;
+  const int64_t D = obj->n_dofs;
+  DevBuf G;
+  if ((rc = G.alloc((size_t)(D * Q) * sizeof(float2), s))) return rc;
+  if ((rc = pi_dof_jacobian(kg.k, b.b, G.p, reinterpret_cast<pi_stream>(s)))) return rc;
+  const int64_t total = D * Q;
+  jacobian_to_qd_kernel<<<(unsigned)((total + 255) / 256), 256, 0, s>>>(static_cast<const float2*>(G.p), Q, D,
+                                                                        reinterpret_cast<double2*>(d_grad_out));
+  PI_LAUNCHED("jacobian_to_qd_kernel");
+  // The reference wrapper returned with the result in place (it synchronised the device).
+  PI_CUDA(cudaStreamSynchronize(s));
+  return PI_OK;
+}
+
+int pi_compute_Ak_gradient_single(const pi_object* obj, const double* k, double* out) {
+  if (!obj || !k || !out || obj->n_dofs <= 0)
+    return fail(PI_ERR_INVALID_ARGUMENT, "pi_compute_Ak_gradient_single: bad arguments");
+  const int64_t D = obj->n_dofs;
+  const double km = std::sqrt(k[0] * k[0] + k[1] * k[1] + k[2] * k[2]);
+  if (km < 1e-10) {  // the reference returns zeros at k = 0 (compute_intersection_volume.cu:586)
+    int rc = validate_object(*obj, 0);
+    if (rc) return rc;
+    std::fill(out, out + 2 * D, 0.0);
+    return PI_OK;
+  }
+  const double dir[3] = {k[0] / km, k[1] / km, k[2] / km};
+  DevBuf d;
+  int rc = d.alloc((size_t)(2 * D) * sizeof(double), cudaStreamPerThread);
+  if (rc) return rc;
+  rc = pi_compute_Ak_gradient(obj, dir, &km, 1, static_cast<double*>(d.p), 256);
+  if (rc) return rc;
+  PI_CUDA(cudaMemcpy(out, d.p, (size_t)(2 * D) * sizeof(double), cudaMemcpyDeviceToHost));
   return PI_OK;
 }
 

@@ -43,6 +43,7 @@
 #include <cuda_runtime.h>
 #include <cstdint>
 #include <algorithm>
+#include <atomic>
 #include <mutex>
 #include <cstring>
 #include "pi_internal.h"
@@ -58,7 +59,10 @@ using namespace tc;
 
 constexpr int GM = GROUP_TILE;
 constexpr int CK = GROUP_CHUNK;
-constexpr int CHAIN = 2;                         // k chunks per tensor-memory accumulation chain
+#ifndef PI_GROUP_CHAIN
+#define PI_GROUP_CHAIN 2
+#endif
+constexpr int CHAIN = PI_GROUP_CHAIN;            // k chunks per tensor-memory accumulation chain
 constexpr int OPB = GM * 128;                    // 16,384 B: one 128 x 64 16-bit operand block
 constexpr int HALF = GM * 128;                   // 16,384 B: 128 rows x 32 FP32 values (one TMA box)
 constexpr int BOXB = 2 * HALF;                   // 32 KB: one tile's FP32 chunk
@@ -158,6 +162,7 @@ group_split3_kernel(const GroupDev g, const __grid_constant__ CUtensorMap xmap) 
   uint8_t* smem = smem_raw + ((1024 - (smem_u32(smem_raw) & 1023)) & 1023);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   int* err = g.err;
+  const long long wlim = g.wait_cycles > 0 ? (long long)g.wait_cycles : WAIT_CYCLES;
   int n_items = g.hdr->n_items;
   if (n_items > g.max_items) {  // descriptor inconsistent with the partial arena: do no work
     if (threadIdx.x == 0 && blockIdx.x == 0) atomicCAS(err, 0, ERR_CAPACITY);
@@ -198,10 +203,11 @@ group_split3_kernel(const GroupDev g, const __grid_constant__ CUtensorMap xmap) 
           for (int c = 0; c < w.nchunks; ++c, ++gc) {
             const int s = (int)(gc % NST);
             const int64_t rnd = gc / NST;
-            if (rnd > 0 && !mbar_wait(smem_u32(&empty_bar[s]), (uint32_t)((rnd - 1) & 1), err, ERR_LOAD)) {
+            if (rnd > 0 && !mbar_wait(smem_u32(&empty_bar[s]), (uint32_t)((rnd - 1) & 1), err, ERR_LOAD, wlim)) {
               ok = false;
               break;
             }
+            if (g.starve_plus1 > 0 && blockIdx.x == 0 && gc + 1 == g.starve_plus1) continue;  // testing: never loaded
             const int x = (int)(((int64_t)w.chunk0 + (int64_t)c * w.cstride) * (2 * CK));  // FP32 column
             const uint32_t st = smem_u32(smem + s * STAGE), bar = smem_u32(&load_bar[s]);
             mbar_expect_tx(bar, diag ? BOXB : 2 * BOXB);  // out-of-range rows and columns arrive as zeros
@@ -215,7 +221,7 @@ group_split3_kernel(const GroupDev g, const __grid_constant__ CUtensorMap xmap) 
           }
         }
         for (int64_t c = max((int64_t)0, issued - NST); c < issued; ++c)
-          mbar_drain(smem_u32(&load_bar[c % NST]), (uint32_t)((c / NST) & 1));
+          mbar_drain(smem_u32(&load_bar[c % NST]), (uint32_t)((c / NST) & 1), wlim);
       }
     } else {
       const int piece = lane & 15, rpar = lane >> 4;
@@ -237,7 +243,7 @@ group_split3_kernel(const GroupDev g, const __grid_constant__ CUtensorMap xmap) 
           const int s = (int)(gc % NST);
           const int64_t rnd = gc / NST;
           // every lane acquires the stage itself before writing into it
-          if (rnd > 0) ok = mbar_wait(smem_u32(&empty_bar[s]), (uint32_t)((rnd - 1) & 1), err, ERR_LOAD);
+          if (rnd > 0) ok = mbar_wait(smem_u32(&empty_bar[s]), (uint32_t)((rnd - 1) & 1), err, ERR_LOAD, wlim);
           ok = __all_sync(0xffffffffu, ok);
           if (!ok) break;
           const int64_t col0 = ((int64_t)w.chunk0 + (int64_t)c * w.cstride) * CK;
@@ -284,7 +290,7 @@ group_split3_kernel(const GroupDev g, const __grid_constant__ CUtensorMap xmap) 
       // Never leave with a copy still landing in shared memory.
       cp_async_wait_all();
       for (int64_t c = max((int64_t)0, issued - NST); c < issued; ++c)
-        mbar_drain(smem_u32(&load_bar[c % NST]), (uint32_t)((c / NST) & 1));
+        mbar_drain(smem_u32(&load_bar[c % NST]), (uint32_t)((c / NST) & 1), wlim);
     }
   } else if (warp < CWARPS) {
     // ---------------- converters ----------------
@@ -315,7 +321,7 @@ group_split3_kernel(const GroupDev g, const __grid_constant__ CUtensorMap xmap) 
       for (int c = 0; c < w.nchunks; ++c, ++gc) {
         const int s = (int)(gc % NST);
         const int64_t rnd = gc / NST;
-        ok = mbar_wait(smem_u32(&load_bar[s]), (uint32_t)(rnd & 1), err, ERR_CONVERT);
+        ok = mbar_wait(smem_u32(&load_bar[s]), (uint32_t)(rnd & 1), err, ERR_CONVERT, wlim);
         ok = __all_sync(0xffffffffu, ok);
         if (!ok) break;
         uint8_t* st = smem + s * STAGE;
@@ -378,11 +384,11 @@ group_split3_kernel(const GroupDev g, const __grid_constant__ CUtensorMap xmap) 
           const int b = (int)(gch & 1);
           const bool first = (c % CHAIN) == 0;
           if (first && gch >= 2) {
-            if (!mbar_wait(smem_u32(&che_bar[b]), (uint32_t)(((gch >> 1) - 1) & 1), err, ERR_MMA)) { ok = false; break; }
+            if (!mbar_wait(smem_u32(&che_bar[b]), (uint32_t)(((gch >> 1) - 1) & 1), err, ERR_MMA, wlim)) { ok = false; break; }
           }
           const int s = (int)(gc % NST);
           const int64_t rnd = gc / NST;
-          if (!mbar_wait(smem_u32(&full_bar[s]), (uint32_t)(rnd & 1), err, ERR_MMA)) { ok = false; break; }
+          if (!mbar_wait(smem_u32(&full_bar[s]), (uint32_t)(rnd & 1), err, ERR_MMA, wlim)) { ok = false; break; }
           fence_after();
           const uint32_t st = smem_u32(smem + s * STAGE);
           const uint64_t aH = desc_sw128(st), aL = desc_sw128(st + OPB);
@@ -405,7 +411,7 @@ group_split3_kernel(const GroupDev g, const __grid_constant__ CUtensorMap xmap) 
       }
       // every MMA issued by this thread has completed before tensor memory is freed
       umma_commit(smem_u32(&fin_bar));
-      mbar_drain(smem_u32(&fin_bar), 0u);
+      mbar_drain(smem_u32(&fin_bar), 0u, wlim);
     }
     __syncwarp();
   } else {
@@ -422,7 +428,9 @@ group_split3_kernel(const GroupDev g, const __grid_constant__ CUtensorMap xmap) 
       float* out = g.partials + (int64_t)it * (GM * GM) + (int64_t)row * GM;
       for (int ch = 0; ch < nch; ++ch, ++gch) {
         const int b = (int)(gch & 1);
-        if (!mbar_wait(smem_u32(&chf_bar[b]), (uint32_t)((gch >> 1) & 1), err, ERR_EPILOGUE)) { ok = false; break; }
+        // every lane takes the same decision before the warp-collective tensor-memory loads
+        ok = __all_sync(0xffffffffu, mbar_wait(smem_u32(&chf_bar[b]), (uint32_t)((gch >> 1) & 1), err, ERR_EPILOGUE, wlim));
+        if (!ok) break;
         fence_after();
         const bool first = ch == 0, last = ch == nch - 1;
 #pragma unroll 1
@@ -543,6 +551,10 @@ __global__ void group_single_setup_kernel(GRow* rows, GQuery* query, GHeader* hd
 
 int g_sms = 0;
 std::once_flag g_attr_once;
+// Testing hooks (pi_test_set_contract_faults): the wait limit and the chunk
+// that CTA 0's loader skips, read when a single-matrix contraction is set up.
+std::atomic<long long> g_test_wait_cycles{0};
+std::atomic<long long> g_test_starve_chunk{-1};
 int g_attr_rc = PI_OK;
 
 int sms() {
@@ -677,7 +689,7 @@ size_t group_single_ws_bytes(int64_t Q, int n, int op) {
 }
 
 int launch_group_single(const float2* Jw, int64_t Q, int n, int op, double* V, void* ws, size_t ws_bytes,
-                        double scale, cudaStream_t s) {
+                        double scale, cudaStream_t s, const float* row_amax) {
   if (n <= 0) return PI_OK;
   if (Q % 2 != 0) return fail(PI_ERR_UNSUPPORTED, "tensor-core contraction needs an even node count");
   if ((reinterpret_cast<uintptr_t>(Jw) & 15) != 0) return fail(PI_ERR_INVALID_ARGUMENT, "J must be 16-byte aligned");
@@ -697,15 +709,21 @@ int launch_group_single(const float2* Jw, int64_t Q, int n, int op, double* V, v
   g.op = op;
   g.phase = 0;
   g.scale = scale;
-  float* amax = nullptr;
-  if (op == GROUP_OP_F16) {
-    amax = reinterpret_cast<float*>(base + p.off_amax);
-    PI_CUDA(cudaMemsetAsync(amax, 0, (size_t)n * sizeof(float), s));
+  g.wait_cycles = g_test_wait_cycles.load();
+  const long long starve = g_test_starve_chunk.load();
+  g.starve_plus1 = starve >= 0 && starve < 0x7ffffffeLL ? (int32_t)(starve + 1) : 0;
+  const float* amax = nullptr;
+  if (op == GROUP_OP_F16 && row_amax) {
+    amax = row_amax;  // the form-factor kernel's row maxima: no second pass over J
+  } else if (op == GROUP_OP_F16) {
+    float* ws_amax = reinterpret_cast<float*>(base + p.off_amax);
+    amax = ws_amax;
+    PI_CUDA(cudaMemsetAsync(ws_amax, 0, (size_t)n * sizeof(float), s));
     const int64_t q4 = Q / 2;  // whole float4s per row (2 complex each); rows start 16-byte aligned
     const int bx = (int)std::max<int64_t>(1, std::min<int64_t>((q4 + 255) / 256, 4 * sms() / n));
     if (q4 > 0) {
       row_amax_kernel<<<dim3((unsigned)bx, (unsigned)n), 256, 0, s>>>(reinterpret_cast<const float4*>(Jw), q4, n,
-                                                                      reinterpret_cast<unsigned*>(amax));
+                                                                      reinterpret_cast<unsigned*>(ws_amax));
       PI_LAUNCHED("row_amax_kernel");
     }
   }
@@ -721,6 +739,11 @@ int launch_group_single(const float2* Jw, int64_t Q, int n, int op, double* V, v
   if (rc) return rc;
   const int64_t red_blocks = std::min<int64_t>(((int64_t)n * n + RED_THREADS - 1) / RED_THREADS, 4 * sms());
   return launch_group_reduce(g, (int)std::max<int64_t>(1, red_blocks), s);
+}
+
+void group_test_set_faults(long long wait_cycles, long long starve_chunk) {
+  g_test_wait_cycles.store(wait_cycles > 0 ? wait_cycles : 0);
+  g_test_starve_chunk.store(starve_chunk);
 }
 
 }  // namespace pi

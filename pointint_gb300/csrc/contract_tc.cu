@@ -216,7 +216,8 @@ syrk_split3_kernel(const __grid_constant__ CUtensorMap xmap, int n, int64_t K, i
 
   // ---------------- epilogue: TMEM -> FP32 partial tile ----------------
   if (warp < 4) {
-    const bool ok = mbar_wait(smem_u32(&done_bar), 0u, err, ERR_EPILOGUE_WAIT);
+    // every lane takes the same decision before the warp-collective tensor-memory loads
+    const bool ok = __all_sync(0xffffffffu, mbar_wait(smem_u32(&done_bar), 0u, err, ERR_EPILOGUE_WAIT));
     fence_after();
     const int row = warp * 32 + lane;
     float* out = partials + ((int64_t)blockIdx.y * gridDim.x + blockIdx.x) * (TC_M * TC_M) + (int64_t)row * TC_M;

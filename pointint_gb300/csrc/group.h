@@ -80,6 +80,9 @@ struct GroupDev {                      // kernel argument; pointers fixed for th
   int* err;                            // 0 = ok
   double* out;                         // output arena
   double scale;                        // 1 / (8 pi^3)
+  int64_t wait_cycles;                 // limit of every bounded wait in SM clocks; <= 0: the built-in ~2 s
+  int32_t starve_plus1;                // testing: > 0 makes CTA 0's loader skip its chunk starve_plus1 - 1
+  int32_t reserved2_;
 };
 
 // Power-of-two operand scale of a row with maximum |x| = amax: the scaled
@@ -143,7 +146,14 @@ int launch_group_reduce(const GroupDev& g, int grid, cudaStream_t s);
 // descriptors (and, for FP16 operands, the row maxima) are formed on the
 // device inside the workspace.
 size_t group_single_ws_bytes(int64_t Q, int n, int op);
+// Testing: every later single-matrix contraction waits at most wait_cycles SM
+// clocks per barrier (<= 0: the built-in ~2 s), and CTA 0's loader skips its
+// chunk starve_chunk (< 0: none), so that a wait runs out.
+void group_test_set_faults(long long wait_cycles, long long starve_chunk);
+// row_amax (optional, FP16 operands only): each row's largest |Re|, |Im| (or
+// any upper bound of it), as written by the form-factor kernel; without it
+// the maxima are found by a pass over J.
 int launch_group_single(const float2* Jw, int64_t Q, int n, int op, double* V, void* ws, size_t ws_bytes,
-                        double scale, cudaStream_t s);
+                        double scale, cudaStream_t s, const float* row_amax = nullptr);
 
 }  // namespace pi

@@ -45,7 +45,8 @@ __device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
 // the grid has recorded an error.  The error flag lives in global memory, so
 // it is polled only every ~10 us of SM clock: a load per spin would put an L2
 // round trip between every barrier completion and the waiter's wake-up.
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, int* err, int code) {
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, int* err, int code,
+                                          long long limit = WAIT_CYCLES) {
   constexpr long long POLL_CYCLES = 20000;
   const long long t0 = clock64();
   long long next = t0 + POLL_CYCLES;
@@ -53,7 +54,7 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, int* er
     const long long now = clock64();
     if (now >= next) {
       if (*reinterpret_cast<volatile int*>(err) != 0) return false;
-      if (now - t0 > WAIT_CYCLES) {
+      if (now - t0 > limit) {
         atomicCAS(err, 0, code);
         return false;
       }
@@ -65,9 +66,9 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, int* er
 
 // Bounded wait used only to drain copies or MMAs already in flight; ignores
 // the error flag.
-__device__ __forceinline__ void mbar_drain(uint32_t bar, uint32_t parity) {
+__device__ __forceinline__ void mbar_drain(uint32_t bar, uint32_t parity, long long limit = WAIT_CYCLES) {
   const long long t0 = clock64();
-  while (!mbar_try_wait(bar, parity) && clock64() - t0 <= WAIT_CYCLES) {
+  while (!mbar_try_wait(bar, parity) && clock64() - t0 <= limit) {
   }
 }
 

@@ -207,6 +207,48 @@ def test_single_k_compute_Ak(cuda, orc):
         assert abs(a - exact) <= 2e-6 * max(1.0, np.linalg.norm(k))
 
 
+@pytest.mark.parametrize("kind", ["ico2_affine", "mesh_dof", "disks_affine", "gauss_affine"])
+def test_registry_gradient_plugin_and_single_k_gradient(cuda, orc, kg29, kind):
+    """pi_compute_Ak_gradient (the registry's gradient function: Q x D
+    complex doubles on the device, dof_cuda_interface.hpp:32-40) and
+    compute_Ak_gradient_cuda (one k-vector, compute_intersection_volume.hpp:129-135)
+    against the oracle's dA(k)/dtheta (affine_dof.cpp:172-322,
+    triangle_mesh_dof.cpp:76-143), within 2e-5 of the largest entry."""
+    from pointint_gb300 import pointint_cpp as pc
+    obj = shapes(kind, np.random.default_rng(KINDS.index(kind)))
+    D = len(obj.dofs)
+    sel = np.arange(0, kg29.num_nodes, 37)
+    dirs, kmag = np.ascontiguousarray(kg29.dirs[sel]), np.ascontiguousarray(kg29.kmag[sel])
+    out = torch.zeros(len(sel) * D * 2, dtype=torch.float64, device="cuda")
+    c = obj.as_c()
+    _lib.check(_lib.lib().pi_compute_Ak_gradient(ctypes.byref(c), dirs.ctypes.data, kmag.ctypes.data, len(sel),
+                                                 ctypes.c_void_p(out.data_ptr()), 256))
+    got = out.cpu().numpy().view(np.complex128).reshape(len(sel), D)
+    ref = orc.form_factor_grad(to_oracle(orc, [obj])[0], dirs * kmag[:, None])
+    err = np.abs(got - ref).max() / np.abs(ref).max()
+    print(f"\n{kind}: registry gradient plugin, {len(sel)} nodes x {D} DoFs: max err {err:.2e}")
+    assert err <= 2e-5, err
+    for q in (0, len(sel) // 2, len(sel) - 1):
+        k = dirs[q] * kmag[q]
+        g1 = pc.compute_Ak_gradient_cuda(obj.geom, k, obj.dof_type, obj.dofs)
+        assert np.abs(g1 - ref[q]).max() <= 2e-5 * np.abs(ref).max()
+    assert not pc.compute_Ak_gradient_cuda(obj.geom, [0.0, 0.0, 0.0], obj.dof_type, obj.dofs).any()
+
+
+def test_cpu_binding_name_returns_the_volume(cuda, orc, kg29):
+    """compute_intersection_volume_cpu (bindings.cpp:63-69) returns the
+    intersection volume (computed by the GPU kernels) rather than raising."""
+    from pointint_gb300 import pointint_cpp as pc
+    Vc, Fc = G.create_unit_cube_mesh()
+    Vs, Fs = G.icosphere(3)
+    g1, g2 = pc.make_triangle_mesh(Vc, Fc), pc.make_triangle_mesh(Vs * 0.7 + 0.2, Fs)
+    v_cpu = pc.compute_intersection_volume_cpu(g1, g2, kg29)
+    v_gpu = pc.compute_intersection_volume_cuda(g1, g2, kg29)
+    ref = orc.pair_volume(orc.Obj(0, g1.elems), orc.Obj(0, g2.elems), (kg29.dirs, kg29.kmag, kg29.w))["volume"]
+    assert v_cpu == v_gpu
+    assert abs(v_cpu - ref) <= VOL_TOL * abs(ref)
+
+
 def test_ball_transform(cuda, orc):
     """Second analytic oracle: icospheres rescaled to the unit ball's volume
     against the exact ball transform A(k) = i|k| F_ball(k)

@@ -108,3 +108,18 @@ def test_tensor_core_contraction_shapes(cuda, n, radial):
         assert np.array_equal(V, V.T), precision
         assert np.isfinite(V).all(), precision
         assert err.max() <= tol, (precision, err.max())
+
+
+def test_form_factor_row_maxima_feed_the_fp16_split(cuda, setup):
+    """The form-factor kernel's row maxima (pi_form_factors_rowmax) equal the
+    rows' largest |Re|, |Im|, and the FP16-split contraction given them is
+    bitwise the one that finds them with its own pass over J."""
+    kg, objs, _ = setup
+    b = core.ObjectBatch(objs)
+    amax = torch.full((len(objs),), -1.0, dtype=torch.float32, device="cuda")
+    J = core.form_factors(kg, b, True, row_amax=amax)
+    ref = torch.view_as_real(J).abs().amax(dim=(1, 2))
+    assert torch.equal(amax, ref)
+    V_pass = core.contract(kg, J, "fp16x3")
+    V_fused = core.contract(kg, J, "fp16x3", row_amax=amax)
+    assert torch.equal(V_pass, V_fused)
