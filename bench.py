@@ -51,8 +51,13 @@ def parse():
     p.add_argument("--cpu-seconds", type=float, default=12.0)
     p.add_argument("--no-serve", action="store_true", help="skip the serving measurements")
     p.add_argument("--no-configs", action="store_true", help="skip the other workload configurations")
-    p.add_argument("--serve-queries", type=int, default=160,
-                   help="scene-stream sample size (the stream workload has 10,000 queries)")
+    p.add_argument("--serve-queries", type=int, default=240,
+                   help="scene-stream sample size (the stream workload has 10,000 queries; see --stream-full)")
+    p.add_argument("--serve-plain-prefix", type=int, default=100,
+                   help="queries of the stream timed one at a time on the plain FP32 path")
+    p.add_argument("--stream-full", action="store_true",
+                   help="only the scene stream at its stated size: 10,000 queries saturated, Poisson arrivals at "
+                        "0.8 of the saturated rate over all of them and at 0.25 / 0.5 over the first 2,000")
     p.add_argument("--serve-burst", type=int, default=200, help="256-object scene queries in the warm burst")
     p.add_argument("--objects", type=int, default=256,
                    help="object count of the matrix workload (256 = the benchmark; smaller only for profiling)")
@@ -307,17 +312,32 @@ def run_gb300(args):
     sm_clock = clocks.get("sm_mhz") or peaks.get("sm_max_mhz", 2070.0)
     n_sm = torch.cuda.get_device_properties(local).multi_processor_count
     ff_avg_s = ff_ms / args.steps / 1e3
-    sfu_achieved = SFU_OPS_PER_EVAL * evals_step / ff_avg_s / 1e9
-    sfu_peak = n_sm * SFU_PER_SM_PER_CLK * float(peaks.get("sm_max_mhz", 2070.0)) * 1e6 / 1e9
+    clk_max = float(peaks.get("sm_max_mhz", 2070.0))
     fp32_achieved = FP32_FLOPS_PER_EVAL * evals_step / ff_avg_s / 1e12
-    fp32_peak = n_sm * FP32_FLOPS_PER_SM_PER_CLK * float(peaks.get("sm_max_mhz", 2070.0)) * 1e6 / 1e12
-    roofline = {"kernel": "ff_kernel", "bound": "sfu", "achieved": sfu_achieved, "peak": sfu_peak, "unit": "Gop/s",
-                "frac": sfu_achieved / sfu_peak, "traffic": FF_TRAFFIC_BYTES_PER_LAUNCH,
+    fp32_peak = n_sm * FP32_FLOPS_PER_SM_PER_CLK * clk_max * 1e6 / 1e12
+    sfu_achieved = SFU_OPS_PER_EVAL * evals_step / ff_avg_s / 1e9
+    sfu_peak = n_sm * SFU_PER_SM_PER_CLK * clk_max * 1e6 / 1e9
+    # issue slots: 4 warp instructions per SM per clock; thread instructions per
+    # evaluation from the kernel's ncu capture on 32 of the 256 objects
+    issue_achieved = FF_THREAD_INSTR_PER_EVAL / 32.0 * evals_step / ff_avg_s / 1e9
+    issue_peak = n_sm * 4 * clk_max * 1e6 / 1e9
+    roofline = {"kernel": "ff_kernel", "bound": "fp32-issue", "achieved": fp32_achieved, "peak": fp32_peak,
+                "unit": "TFLOP/s", "frac": fp32_achieved / fp32_peak, "traffic": FF_TRAFFIC_BYTES_PER_LAUNCH,
                 "kernel_ms": ff_avg_s * 1e3, "share_of_step": (ff_ms / total_ms) if world == 1 else None,
-                "algorithmic_unit": f"{SFU_OPS_PER_EVAL} SFU ops per triangle x k evaluation x {evals_step:.4e} evaluations",
-                "peak_source": f"nominal {SFU_PER_SM_PER_CLK} MUFU/clk/SM x {n_sm} SMs x {peaks.get('sm_max_mhz', 2070.0)} MHz "
-                               f"(MEASURED_PEAKS.json has no SFU/FP32 figure; {peak_src} file)",
-                "fp32": {"achieved": fp32_achieved, "peak": fp32_peak, "unit": "TFLOP/s", "frac": fp32_achieved / fp32_peak}}
+                "algorithmic_unit": f"{FP32_FLOPS_PER_EVAL} FP32 flops (FMA = 2) per triangle x k evaluation, the "
+                                    f"reference algorithm's count, x {evals_step:.4e} evaluations",
+                "peak_source": f"nominal FP32: {FP32_FLOPS_PER_SM_PER_CLK} flops/clk/SM x {n_sm} SMs x {clk_max} MHz "
+                               "(MEASURED_PEAKS.json holds HBM and bf16 tensor peaks only)",
+                "binding": "instruction issue of the FP32 pipe: the kernel uses no MUFU (SFU) instructions; its "
+                           "sine/cosine are a phasor table and polynomials",
+                "issue": {"thread_instructions_per_evaluation": FF_THREAD_INSTR_PER_EVAL,
+                          "achieved": issue_achieved, "peak": issue_peak, "unit": "G warp-instructions/s",
+                          "frac": issue_achieved / issue_peak,
+                          "source": "instructions per evaluation from ncu (smsp__inst_executed.sum x 32 / "
+                                    "evaluations, 32-object capture); rate from this run's CUDA events"},
+                "sfu_count": {"achieved": sfu_achieved, "peak": sfu_peak, "unit": "Gop/s", "frac": sfu_achieved / sfu_peak,
+                              "note": f"{SFU_OPS_PER_EVAL} SFU-class operations per evaluation in the reference "
+                                      "algorithm (accounting only: this kernel issues none)"}}
 
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -356,6 +376,9 @@ def run_gb300(args):
 # J (256 x 76,928 complex64 = 157.5 MB) exceeds the 129 MB L2 and is counted
 # as written once.
 FF_TRAFFIC_BYTES_PER_LAUNCH = 5.69e6 * 656896 / 82112 + 256 * 76928 * 8
+# Thread instructions per triangle x k evaluation of ff_kernel, from its ncu
+# capture on 32 of the 256 objects (smsp__inst_executed.sum x 32 / 6.32e9).
+FF_THREAD_INSTR_PER_EVAL = 69.2
 
 
 def _pcts(ms):
@@ -425,6 +448,8 @@ def configs_bench(args, flush):
     out["large_mesh"] = {"workload": meta3["workload"], "sample_objects": len(objs3), "n_k": kg3.num_nodes,
                          "ms": ms, "tri_k_evals_per_s": evals3 / (ms / 1e3),
                          "full_config_seconds_at_this_rate": 32 * meta3["n_triangles_each"] * kg3.num_nodes / (evals3 / (ms / 1e3))}
+    core.form_factors(kg3, b3, False, out=J3)
+    out["large_mesh"].update(oracle_check(J3, objs3, kg3, 1600))
     del b3, J3
     # surfels sample: forward and backward
     kg4, objs4, meta4 = configs.surfels64(n_objects=8)
@@ -446,9 +471,38 @@ def configs_bench(args, flush):
     out["surfels64"] = {"workload": meta4["workload"], "sample_objects": len(objs4), "forward_ms": ms_f,
                         "forward_disk_k_evals_per_s": evals4 / (ms_f / 1e3), "forward_backward_ms": ms_fb,
                         "backward_over_forward": (ms_fb - ms_f) / ms_f}
+    out["surfels64"].update(oracle_check(core.form_factors(kg4, scene.batch, False), objs4, kg4, 1500))
     del scene
     out["hessian256"], out["align"] = hessian_align_bench(flush)
     return out
+
+
+def oracle_check(J, objs, kg, n_nodes):
+    """Form factors of the GPU (J [n, Q], unscaled) against the FP64 oracle at
+    n_nodes evenly strided k-nodes (every radius band included), and the
+    volumes contracted over those nodes from either J."""
+    try:
+        from oracle import oracle as orc
+        Q = kg.num_nodes
+        sel = np.unique(np.linspace(0, Q - 1, n_nodes).astype(np.int64))
+        Jg = J[:, torch_index(sel)].cpu().numpy()
+        Jo = orc.form_factor_matrix([orc.Obj(o.geom.type, o.geom.elems, o.dof_type, o.dofs) for o in objs],
+                                    kg.dirs[sel], kg.kmag[sel]).T
+        w = kg.w[sel]
+        Vg = ((Jg * w) @ Jg.conj().T).real / (8 * np.pi ** 3)
+        Vo = ((Jo * w) @ Jo.conj().T).real / (8 * np.pi ** 3)
+        d = np.sqrt(np.abs(np.outer(np.diag(Vo), np.diag(Vo))))
+        return {"oracle_sample_nodes": int(len(sel)), "kmax_sampled": float(kg.kmag[sel].max()),
+                "J_rel_err_vs_oracle": float(np.linalg.norm(Jg - Jo) / np.linalg.norm(Jo)),
+                "max_rel_err_vs_oracle": float((np.abs(Vg - Vo) / np.maximum(np.abs(Vo), 1e-3 * d)).max()),
+                "error_definition": "volumes over the sampled nodes: max_ij |dV_ij| / max(|V_ij|, 1e-3 sqrt(V_ii V_jj))"}
+    except Exception as exc:  # the oracle must not break the GPU line
+        return {"max_rel_err_vs_oracle": f"oracle unavailable: {exc}"}
+
+
+def torch_index(sel):
+    import torch
+    return torch.as_tensor(sel, device="cuda")
 
 
 def hessian_align_bench(flush):
@@ -465,11 +519,21 @@ def hessian_align_bench(flush):
     ms_j = _timed(lambda: core.dof_jacobian(kg, b, out=Gm), flush, reps=2)
     H = {}
     ms_h = _timed(lambda: H.__setitem__("H", core.contract(kg, Gm, "fp32")), flush, reps=2)
+    ms_h16 = _timed(lambda: H.__setitem__("H16", core.contract(kg, Gm, "fp16x3")), flush, reps=2)
+    H32, H16 = H["H"], H["H16"]
+    dH = torch.sqrt(torch.outer(torch.diagonal(H32), torch.diagonal(H32)).abs())
+    err16 = ((H16 - H32).abs() / torch.maximum(H32.abs(), 1e-3 * dH)).max().item()
+    D = Gm.shape[0]
     hess = {"workload": meta["workload"] + "; Gauss-Newton Hessian over all 12 x 256 AffineDoFs",
-            "dofs": int(Gm.shape[0]), "jacobian_ms": ms_j, "contraction_ms": ms_h,
+            "dofs": int(D), "jacobian_ms": ms_j, "contraction_ms": ms_h,
             "jacobian_tri_k_evals_per_s": meta["n_triangles"] * kg.num_nodes / (ms_j / 1e3),
-            "contraction_tflops": 4.0 * kg.num_nodes * Gm.shape[0] ** 2 / (ms_h / 1e3) / 1e12}
-    del Gm, b, H
+            "contraction_tflops": 4.0 * kg.num_nodes * D ** 2 / (ms_h / 1e3) / 1e12,
+            "contraction_fp16x3_ms": ms_h16,
+            "contraction_fp16x3_max_rel_err_vs_fp32": err16,
+            "contraction_error_definition": "max_ij |dH_ij| / max(|H_ij|, 1e-3 sqrt(H_ii H_jj)), FP16x3 against "
+                                            "the FP32 contraction of the same Jacobian rows",
+            "contraction_flops_definition": "4 N_k D^2 (full matrix)"}
+    del Gm, b, H, H32, H16
     torch.cuda.empty_cache()
     rng = np.random.default_rng(0)
     V, F = G.icosphere(4)
@@ -585,41 +649,75 @@ def serving_bench(args, kg, objs, batch, contraction, flush):
         "batches": st["batches"], "graph_launches": st["graph_launches"],
         "tuned_items_per_sm": st["tuned_items_per_sm"]}
 
-    # scene stream sample
-    _, lib, queries, _, meta = configs.serving_stream(seed=2, n_queries=args.serve_queries, kgrid=False)
+    out["scene_stream"] = stream_bench(kg, args.serve_queries, rates=(0.5,), poisson_queries=args.serve_queries,
+                                       plain_prefix=args.serve_plain_prefix)
+    return out
+
+
+def stream_bench(kg, n_queries, rates=(0.5,), poisson_queries=None, plain_prefix=100, seed=2):
+    """The scene stream (N ~ logU[2,512] library objects per query, translations
+    N(0,0.5^2), rotations with probability 0.2): n_queries submitted at once
+    (saturated throughput and latency), then open-loop Poisson arrivals at each
+    fraction of the saturated rate in `rates` over the first poisson_queries
+    queries, against one-query-at-a-time plain FP32 (every form factor
+    evaluated, FP32 contraction) on the first plain_prefix queries.  Latency is
+    host wall-clock from submission to the result written."""
+    import threading
+    import torch
+    from pointint_gb300 import configs, core, geometry as G
+    from pointint_gb300.serving import Server
+    _, lib, queries, _, meta = configs.serving_stream(seed=seed, n_queries=n_queries, kgrid=False)
+    poisson_queries = min(poisson_queries or n_queries, n_queries)
+    out = {"workload": meta["workload"], "queries": n_queries, "mean_objects": meta["mean_objects"],
+           "precision": "fp16x3"}
     with Server(kg, lib, precision="fp16x3") as srv:
         srv.query(np.arange(len(lib), dtype=np.int32), None, None)  # library rows resident
+        st0 = srv.stats()
         t0 = time.perf_counter()
         ts = [srv.submit(*q) for q in queries]
+        lat = []
         for t in ts:
             srv.wait(t)
+            a, _, c = srv.times(t)
+            lat.append((c - a) / 1e6)
+            srv.release(t)
         sat_s = time.perf_counter() - t0
-        sat_lat = [(srv.times(t)[2] - srv.times(t)[0]) / 1e6 for t in ts]
-        qps = len(queries) / sat_s
-        # open-loop Poisson arrivals at half the saturated rate
-        half = queries[: max(1, len(queries) // 2)]
-        gaps = np.random.default_rng(3).exponential(2.0 / qps, size=len(half))
-        tickets = []
-
-        def feed():
-            t_start = time.perf_counter()
-            due = np.cumsum(gaps)
-            for k, q in enumerate(half):
-                dt = due[k] - (time.perf_counter() - t_start)
-                if dt > 0:
-                    time.sleep(dt)
-                tickets.append(srv.submit(*q))
-
-        th = threading.Thread(target=feed)
-        th.start()
-        th.join()
-        for t in tickets:
-            srv.wait(t)
-        poi_lat = [(srv.times(t)[2] - srv.times(t)[0]) / 1e6 for t in tickets]
+        qps = n_queries / sat_s
         st = srv.stats()
+        out.update(saturated_queries_per_s=qps, saturated_latency=_pcts(lat),
+                   evaluations=st["evaluations"] - st0["evaluations"], batches=st["batches"] - st0["batches"])
+        sweep = []
+        for frac in rates:
+            sub = queries[:poisson_queries]
+            gaps = np.random.default_rng(3).exponential(1.0 / (frac * qps), size=len(sub))
+            tickets = []
+
+            def feed():
+                t_start = time.perf_counter()
+                due = np.cumsum(gaps)
+                for k, q in enumerate(sub):
+                    dt = due[k] - (time.perf_counter() - t_start)
+                    if dt > 0:
+                        time.sleep(dt)
+                    tickets.append(srv.submit(*q))
+
+            th = threading.Thread(target=feed)
+            t1 = time.perf_counter()
+            th.start()
+            th.join()
+            lat = []
+            for t in tickets:
+                srv.wait(t)
+                a, _, c = srv.times(t)
+                lat.append((c - a) / 1e6)
+                srv.release(t)
+            span = time.perf_counter() - t1
+            sweep.append({"rate_fraction_of_saturated": frac, "offered_queries_per_s": frac * qps,
+                          "achieved_queries_per_s": len(sub) / span, "queries": len(sub), "latency": _pcts(lat)})
+        out["poisson"] = sweep
     # one query at a time, plain FP32: every form factor evaluated, FP32 contraction
     base = []
-    for objects, rot, trans in queries[:8]:
+    for objects, rot, trans in queries[:plain_prefix]:
         sc = [G.SceneObject(lib[o].geom, lib[o].dof_type, G.affine_dofs(rot[k], trans[k]))
               for k, o in enumerate(objects)]
         torch.cuda.synchronize()
@@ -627,13 +725,10 @@ def serving_bench(args, kg, objs, batch, contraction, flush):
         core.volume_matrix(kg, sc, "fp32")
         torch.cuda.synchronize()
         base.append(time.perf_counter() - t0)
-    out["scene_stream"] = {
-        "workload": meta["workload"], "sample_queries": len(queries), "mean_objects": meta["mean_objects"],
-        "saturated_queries_per_s": qps, "saturated_latency": _pcts(sat_lat),
-        "poisson_rate_hz": qps / 2, "poisson_latency": _pcts(poi_lat),
-        "plain_fp32_one_at_a_time_queries_per_s": len(base) / sum(base), "plain_fp32_sample": len(base),
-        "speedup_vs_plain_fp32_one_at_a_time": qps * sum(base) / len(base),
-        "evaluations": st["evaluations"], "batches": st["batches"], "precision": "fp16x3"}
+    if base:
+        out.update(plain_fp32_one_at_a_time_queries_per_s=len(base) / sum(base), plain_fp32_prefix=len(base),
+                   plain_fp32_latency=_pcts([b * 1e3 for b in base]),
+                   speedup_vs_plain_fp32_one_at_a_time=qps * sum(base) / len(base))
     return out
 
 
@@ -719,6 +814,19 @@ def profile_case(name: str):
 
 def main():
     args = parse()
+    if args.stream_full:
+        import torch
+        from pointint_gb300.kgrid import standard_kgrid
+        torch.cuda.set_device(0)
+        line = {"mode": "scene stream, full size", "metric": "queries/s; p50/p99 latency ms",
+                "stream": None}
+        kg = standard_kgrid(59, 64)
+        res = stream_bench(kg, 10000, rates=(0.8,), poisson_queries=10000, plain_prefix=args.serve_plain_prefix)
+        low = stream_bench(kg, 2000, rates=(0.25, 0.5), poisson_queries=2000, plain_prefix=0)
+        res["poisson"] = low["poisson"] + res["poisson"]
+        line["stream"] = res
+        print(json.dumps(line))
+        return
     if args.profile_case:
         profile_case(args.profile_case)
         return
