@@ -379,8 +379,9 @@ def run_gb300(args):
 # as written once.
 FF_TRAFFIC_BYTES_PER_LAUNCH = 5.69e6 * 656896 / 82112 + 256 * 76928 * 8
 # Thread instructions per triangle x k evaluation of ff_kernel, from its ncu
-# capture on 32 of the 256 objects (smsp__inst_executed.sum x 32 / 6.32e9).
-FF_THREAD_INSTR_PER_EVAL = 69.2
+# capture on 32 of the 256 objects (smsp__inst_executed.sum 1.213e10 x 32 /
+# 6.317e9 evaluations).
+FF_THREAD_INSTR_PER_EVAL = 61.5
 
 
 def _pcts(ms):
@@ -650,7 +651,7 @@ def serving_bench(args, kg, objs, batch, contraction, flush):
         "fp32_contraction_only_vol_matrix_per_s": (1e3 / fp32_contract_ms) if fp32_contract_ms else None,
         "speedup_vs_fp32_contraction_only": (vps * fp32_contract_ms / 1e3) if fp32_contract_ms else None,
         "batches": st["batches"], "graph_launches": st["graph_launches"],
-        "tuned_items_per_sm": st["tuned_items_per_sm"]}
+        "tuned_items_per_sm": st["tuned_items_per_sm"], "tuned_k_splits": st["tuned_k_splits"]}
 
     out["scene_stream"] = stream_bench(kg, args.serve_queries, rates=(0.5,), poisson_queries=args.serve_queries,
                                        plain_prefix=args.serve_plain_prefix)

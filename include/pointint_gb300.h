@@ -354,6 +354,7 @@ typedef struct {
   int64_t batches, evaluations, resident_hits, resident_misses, evictions;
   int64_t pool_rows, resident_rows, graph_launches;
   int32_t tuned_items_per_sm[4];  /* autotuned work items per SM for scenes of <= 16, <= 128, <= 512, > 512 objects, x 1/4 */
+  int32_t tuned_k_splits[4];      /* the K splits per tile pair that this sets for scenes of 16, 128, 512, 1024 objects */
 } pi_server_stats;
 
 /* Zero config fields take the defaults above. */

@@ -56,7 +56,7 @@ class ServerStats(ctypes.Structure):
     _fields_ = [(n, ctypes.c_int64) for n in ("submitted", "completed", "failed", "cancelled", "batches",
                                              "evaluations", "resident_hits", "resident_misses", "evictions",
                                              "pool_rows", "resident_rows", "graph_launches")] + \
-               [("tuned_items_per_sm", ctypes.c_int32 * 4)]
+               [("tuned_items_per_sm", ctypes.c_int32 * 4), ("tuned_k_splits", ctypes.c_int32 * 4)]
 
 
 class OptimizationState(ctypes.Structure):

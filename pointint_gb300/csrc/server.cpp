@@ -1018,6 +1018,8 @@ int pi_server_stats_get(pi_server s, pi_server_stats* out) {
   st.pool_rows = s->pool_rows;
   st.resident_rows = (int64_t)s->resident.size();
   for (int i = 0; i < 4; ++i) st.tuned_items_per_sm[i] = s->tuned[i];
+  const int rep_n[4] = {16, 128, 512, 1024};
+  for (int i = 0; i < 4; ++i) st.tuned_k_splits[i] = nsplit_for(*s, rep_n[i]);
   *out = st;
   return PI_OK;
 }

@@ -92,8 +92,10 @@ class Server:
     def stats(self) -> dict:
         st = ServerStats()
         check(_lib.lib().pi_server_stats_get(self._h, ctypes.byref(st)))
-        out = {name: getattr(st, name) for name, _ in ServerStats._fields_ if name != "tuned_items_per_sm"}
+        out = {name: getattr(st, name) for name, _ in ServerStats._fields_
+               if name not in ("tuned_items_per_sm", "tuned_k_splits")}
         out["tuned_items_per_sm"] = [v / 4 for v in st.tuned_items_per_sm]
+        out["tuned_k_splits"] = list(st.tuned_k_splits)
         return out
 
     def query(self, objects, rotations=None, translations=None) -> np.ndarray:
