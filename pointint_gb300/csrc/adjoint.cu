@@ -100,6 +100,17 @@ struct AdjStage {
   double so[ADJ_DT];  // dir . origin
 };
 
+// Per-CTA copies of the radii (double-float |k|, and |k| in 1/256 turns per
+// unit length for the table phasors) and of the phasor table; the first
+// __syncthreads of the direction loop publishes them.
+__device__ __forceinline__ void stage_radii(const KGridDev& kg, float2* km, float2* kt, float2* ctab) {
+  for (int r = threadIdx.x; r < kg.L; r += blockDim.x) {
+    km[r] = kg.kmag[r];
+    kt[r] = kg.kt256[r];
+  }
+  for (int t = threadIdx.x; t < 256; t += blockDim.x) ctab[t] = kg.cis_tab[t];
+}
+
 __device__ __forceinline__ void stage_tile(AdjStage& st, const KGridDev& kg, const ObjDev& od, const float2* Bw_obj,
                                            const float2* km, int j0) {
   const int tid = threadIdx.x;
@@ -150,13 +161,13 @@ __global__ void __launch_bounds__(ADJ_THREADS)
 adj_surf_kernel(KGridDev kg, BatchDev b, const AdjWork* __restrict__ work, const float2* __restrict__ Bw,
                 float* __restrict__ out) {
   __shared__ AdjStage st;
-  __shared__ float2 km[ADJ_LMAX];
+  __shared__ float2 km[ADJ_LMAX], kt[ADJ_LMAX], ctab[256];
   const AdjWork wk = work[blockIdx.x];
   const ObjDev od = b.objs[wk.obj];
   const int e = wk.first + threadIdx.x;
   const bool valid = e < od.n_elems;
   const bool disk = od.type == PI_GEOM_DISK;
-  for (int r = threadIdx.x; r < kg.L; r += blockDim.x) km[r] = kg.kmag[r];
+  stage_radii(kg, km, kt, ctab);
   float4 q0 = make_float4(0.f, 0.f, 0.f, 0.f), q1 = q0, ql = q0, nr = q0;
   if (valid) {
     q0 = b.surf_pool[2 * (od.elem_off + e)];
@@ -193,7 +204,7 @@ adj_surf_kernel(KGridDev kg, BatchDev b, const AdjWork* __restrict__ work, const
       for (int r = 0; r < kg.L; ++r) {
         const float2 Bv = Bj[r];
         const df k = df{km[r].x, km[r].y};
-        const cf P = cis(df_mul_un(k, sc));
+        const cf P = cis_tab_df(ctab, kt[r], sc);
         const float ure = Bv.x * P.re + Bv.y * P.im;  // Re(conj(B) P)
         const float uim = Bv.x * P.im - Bv.y * P.re;  // Im(conj(B) P)
         const float k2 = k.hi * k.hi;
@@ -229,12 +240,12 @@ __global__ void __launch_bounds__(ADJ_THREADS, 4)
 adj_tri_kernel(KGridDev kg, BatchDev b, const AdjWork* __restrict__ work, const float2* __restrict__ Bw,
                float* __restrict__ out) {
   __shared__ AdjStage st;
-  __shared__ float2 km[ADJ_LMAX];
+  __shared__ float2 km[ADJ_LMAX], kt[ADJ_LMAX], ctab[256];
   const AdjWork wk = work[blockIdx.x];
   const ObjDev od = b.objs[wk.obj];
   const int e = wk.first + threadIdx.x;
   const bool valid = e < od.n_elems;
-  for (int r = threadIdx.x; r < kg.L; r += blockDim.x) km[r] = kg.kmag[r];
+  stage_radii(kg, km, kt, ctab);
   float4 q0 = make_float4(0.f, 0.f, 0.f, 0.f), q1 = q0, q2 = q0, ql = q0;
   if (valid) {
     q0 = b.tri_pool[3 * (od.elem_off + e)];
@@ -271,7 +282,7 @@ adj_tri_kernel(KGridDev kg, BatchDev b, const AdjWork* __restrict__ work, const 
         if (k.hi < kthr) {
           // F = P SF, D_v = P SV with the series as polynomials in k; with
           // BP = conj(B) P, Re(conj(B) X) = Re(BP SX) and D_a = i F - D_b - D_c
-          const cf P = cis(df_mul_un(k, sm));
+          const cf P = cis_tab_df(ctab, kt[r], sm);
           const float u = k.hi * k.hi, k3 = u * k.hi;
           const float fre = poly_u(cp.fa, u), fim = k3 * poly_u(cp.fb, u);
           const float bim = poly_u(cp.ba, u), bre = k.hi * poly_u(cp.bb, u);
@@ -284,7 +295,7 @@ adj_tri_kernel(KGridDev kg, BatchDev b, const AdjWork* __restrict__ work, const 
           tb = fmaf(k.hi, b_re, tb);
           tc = fmaf(k.hi, c_re, tc);
         } else {
-          const TriDer d = tri_generic_der_at(k, sa, sb, sc, k.hi * d1.hi, k.hi * d2.hi);
+          const TriDer d = tri_generic_der_at(ctab, kt[r], sa, sb, sc, k.hi * d1.hi, k.hi * d2.hi);
           // Re(conj(B) X) = B.re X.re + B.im X.im
           t0 = fmaf(Bv.x, d.F.re, fmaf(Bv.y, d.F.im, t0));
           ta = fmaf(k.hi, fmaf(Bv.x, d.Da.re, Bv.y * d.Da.im), ta);

@@ -216,8 +216,7 @@ __device__ __forceinline__ cf cis_tab_frac(const float2* tab, int idx, float f) 
 // product to ~2^-25 of a unit; the cross terms are added to it (the lo.lo
 // term, ~2^-48 relative, is dropped).
 __device__ __forceinline__ cf cis_tab_df(const float2* tab, float2 kt, df sm) {
-  const float y = kt.x * sm.hi;
-  const float t = y + PI_ROUND_SHIFT;
+  const float t = fmaf(kt.x, sm.hi, PI_ROUND_SHIFT);  // rounds the exact product to an integer
   const float n = t - PI_ROUND_SHIFT;
   float f = fmaf(kt.x, sm.hi, -n);
   f = fmaf(kt.x, sm.lo, f);
@@ -227,12 +226,35 @@ __device__ __forceinline__ cf cis_tab_df(const float2* tab, float2 kt, df sm) {
 
 // The same for an FP32 dot product d (kt still double-float).
 __device__ __forceinline__ cf cis_tab_f(const float2* tab, float2 kt, float d) {
-  const float y = kt.x * d;
-  const float t = y + PI_ROUND_SHIFT;
+  const float t = fmaf(kt.x, d, PI_ROUND_SHIFT);
   const float n = t - PI_ROUND_SHIFT;
   float f = fmaf(kt.x, d, -n);
   f = fmaf(kt.y, d, f);
   return cis_tab_frac(tab, __float_as_int(t) & 255, f);
+}
+
+// Two phasors at once with packed FP32 (sm_100 family): radii a, b in the
+// halves of kth = (kt_a.hi, kt_b.hi), ktl = (kt_a.lo, kt_b.lo), the same dot
+// product in both halves of smh, sml.  Every packed operation is an operation
+// of cis_tab_df on each half, so each half gives cis_tab_df's result.
+struct cf2 { float2 re, im; };
+
+__device__ __forceinline__ float2 neg2(float2 a) { return make_float2(-a.x, -a.y); }
+__device__ __forceinline__ float2 dup2(float a) { return make_float2(a, a); }
+
+__device__ __forceinline__ cf2 cis_tab_df2(const float2* tab, float2 kth, float2 ktl, float2 smh, float2 sml) {
+  const float2 t = __ffma2_rn(kth, smh, dup2(PI_ROUND_SHIFT));
+  const float2 mn = __ffma2_rn(t, dup2(-1.0f), dup2(PI_ROUND_SHIFT));  // -n, exact
+  float2 f = __ffma2_rn(kth, smh, mn);
+  f = __ffma2_rn(kth, sml, f);
+  f = __ffma2_rn(ktl, smh, f);
+  const float2 f2 = __fmul2_rn(f, f);
+  const float2 cm = __fmul2_rn(f2, dup2(-PI_TURN256_C2));
+  const float2 sn = __fmul2_rn(f, __ffma2_rn(f2, dup2(-PI_TURN256_C3), dup2(PI_TURN256)));
+  const float2* ta = tab + (__float_as_int(t.x) & 255);
+  const float2* tb = tab + (__float_as_int(t.y) & 255);
+  const float2 tx = make_float2(ta->x, tb->x), ty = make_float2(ta->y, tb->y);
+  return {__ffma2_rn(tx, cm, __ffma2_rn(neg2(ty), sn, tx)), __ffma2_rn(ty, cm, __ffma2_rn(tx, sn, ty))};
 }
 
 __device__ __forceinline__ cf cmul(cf a, cf b) { return {a.re * b.re - a.im * b.im, a.re * b.im + a.im * b.re}; }
@@ -332,10 +354,41 @@ __device__ __forceinline__ cf tri_series_eval(const TriPoly& t, float u, float k
   return {re, im};
 }
 
+// The coefficients that tri_series_eval_short reads (a[0..3], b[0..2]) alone.
+struct TriPolyShort { float a[4], b[3]; };
+
+__device__ __forceinline__ TriPolyShort tri_series_coeffs_short(float s1, float s2, float g) {
+  const float da = -(s1 + s2) * (1.0f / 3.0f);
+  const float db = s1 + da, dc = s2 + da;
+  const float mu = 0.5f * (da * da + db * db + dc * dc);
+  const float nu = da * db * dc;
+  const float G2 = mu * g, G3 = nu * g, G4 = mu * G2;
+  const float G5 = fmaf(mu, G3, nu * G2);
+  const float G6 = fmaf(mu, G4, nu * G3);
+  const float G7 = fmaf(mu, G5, nu * G4);
+  TriPolyShort t;
+  t.a[0] = -0.5f * g;
+  t.a[1] = G2 * (1.0f / 24.0f);
+  t.a[2] = G4 * (-1.0f / 720.0f);
+  t.a[3] = G6 * (1.0f / 40320.0f);
+  t.b[0] = G3 * (1.0f / 120.0f);
+  t.b[1] = G5 * (-1.0f / 5040.0f);
+  t.b[2] = G7 * (1.0f / 362880.0f);
+  return t;
+}
+
+// tri_series_eval_short for two radii (u = k^2, k3 = k^3 per half) with packed FP32.
+__device__ __forceinline__ cf2 tri_series_eval_short2(const TriPolyShort& t, float2 u, float2 k3) {
+  const float2 re = __ffma2_rn(u, __ffma2_rn(u, __ffma2_rn(u, dup2(t.a[3]), dup2(t.a[2])), dup2(t.a[1])), dup2(t.a[0]));
+  const float2 im = __fmul2_rn(k3, __ffma2_rn(u, __ffma2_rn(u, dup2(t.b[2]), dup2(t.b[1])), dup2(t.b[0])));
+  return {re, im};
+}
+
 // The same series cut after a[3] and b[2], for k |e|max < 1 (|e|max the longest
 // edge, so k sp < 1): the dropped terms stay below 6.2e-9 of |a[0]| (FP64
 // evaluation over icosphere and box triangles at the bound).
-__device__ __forceinline__ cf tri_series_eval_short(const TriPoly& t, float u, float k3) {
+template <class Poly>
+__device__ __forceinline__ cf tri_series_eval_short(const Poly& t, float u, float k3) {
   const float re = fmaf(u, fmaf(u, fmaf(u, t.a[3], t.a[2]), t.a[1]), t.a[0]);
   const float im = k3 * fmaf(u, fmaf(u, t.b[2], t.b[1]), t.b[0]);
   return {re, im};
@@ -357,29 +410,31 @@ __device__ __forceinline__ cf dd1(cf Pu, cf Pv, float g) {
   return {b ? big.re : -m.im * sc, b ? big.im : m.re * sc};
 }
 
-// tri_generic: spread D >= 2.  (f[R,Q] - f[P,R]) / (Q - P) with (P, Q) the pair
-// of vertices with the largest gap (|Q-P| = D, so the subtraction loses at
-// most a factor ~1/D of FP32 precision) and stable first differences.
-// Returns e[pa, pb, pc] given the vertex phasors and al = pb-pa, be = pc-pa.
-// The roles (P, Q, R) are chosen by selects, not a three-way branch: the lanes
-// of a warp hold different directions and pick different pairs, and a branch
-// would run all three cases for the warp.
+// tri_generic: spread D >= 2.  e[u, v, w] = (f[v, w] - f[u, v]) / (w - u)
+// with (u, v) the pair of vertices with the smallest gap.  The two gaps to w
+// are then the middle one and D, both at least D / 2 >= 1, so f[v, w] takes
+// the direct form (Pw - Pv) / (w - v) and the final division is by at least
+// D / 2 (at most a factor 2 more FP32 rounding than a division by D), while
+// f[u, v] takes dd1 (its gap may be anything up to D / 2).  Returns
+// e[pa, pb, pc] given the vertex phasors and al = pb - pa, be = pc - pa.  The
+// roles are chosen by selects, not a three-way branch: the lanes of a warp
+// hold different directions and pick different pairs, and a branch would run
+// all three cases for the warp.
 __device__ __forceinline__ cf tri_generic(cf Pa, cf Pb, cf Pc, float al, float be) {
-  const float gab = al, gac = be, gbc = be - al;
-  const float aab = fabsf(gab), aac = fabsf(gac), abc = fabsf(gbc);
-  const bool c1 = aab >= aac && aab >= abc;  // P = a, Q = b, R = c
-  const bool c2 = !c1 && aac >= abc;         // P = a, Q = c, R = b; else P = b, Q = c, R = a
-  // f[R, Q] = dd1(u1, v1, g1), f[P, R] = dd1(u2, v2, g2)
-  const cf u1 = c1 ? Pc : (c2 ? Pb : Pa);
-  const cf v1 = c1 ? Pb : Pc;
-  const float g1 = c1 ? -gbc : (c2 ? gbc : gac);
-  const cf u2 = c1 || c2 ? Pa : Pb;
-  const cf v2 = c1 ? Pc : (c2 ? Pb : Pa);
-  const float g2 = c1 ? gac : (c2 ? gab : -gab);
-  const float den = c1 ? gab : (c2 ? gac : gbc);
-  const cf fRQ = dd1(u1, v1, g1), fPR = dd1(u2, v2, g2);
-  const float s = rcp_fast(den);
-  return {(fRQ.re - fPR.re) * s, (fRQ.im - fPR.im) * s};
+  const float aab = fabsf(al), aac = fabsf(be), abc = fabsf(be - al);
+  const bool nab = aab <= aac && aab <= abc;  // near pair (a, b), w = c
+  const bool nac = !nab && aac <= abc;        // near pair (a, c), w = b; else (b, c), w = a
+  // vertices as (phasor, phase relative to a)
+  const bool ua = nab || nac;
+  const cf Pu = ua ? Pa : Pb;
+  const cf Pv = nab ? Pb : Pc;
+  const cf Pw = nab ? Pc : (nac ? Pb : Pa);
+  const float zu = ua ? 0.f : al, zv = nab ? al : be, zw = nab ? be : (nac ? al : 0.f);
+  const cf fuv = dd1(Pu, Pv, zv - zu);
+  const float ivw = rcp_fast(zw - zv);
+  const cf fvw = {(Pw.re - Pv.re) * ivw, (Pw.im - Pv.im) * ivw};
+  const float s = rcp_fast(zw - zu);
+  return {(fvw.re - fuv.re) * s, (fvw.im - fuv.im) * s};
 }
 
 }  // namespace pi

@@ -200,13 +200,17 @@ __device__ __forceinline__ float4 ld_shared_f4(const float4* p) {
 
 template <int R>
 struct Acc {
-  float re[R], im[R];  // current chunk
-  float* run;          // run[(4 i + v) FF_THREADS]: v = sum re, sum im, compensation re, im
+  static_assert(R % 2 == 0, "radii are paired for packed FP32");
+  // current chunk; radii (2p, 2p + 1) in one float2, the operand of packed FP32
+  float2 re2[R / 2], im2[R / 2];
+  float* run;  // run[(4 i + v) FF_THREADS]: v = sum re, sum im, compensation re, im
+  __device__ __forceinline__ float& re(int i) { return (i & 1) ? re2[i >> 1].y : re2[i >> 1].x; }
+  __device__ __forceinline__ float& im(int i) { return (i & 1) ? im2[i >> 1].y : im2[i >> 1].x; }
   __device__ __forceinline__ void init(float* base) {
     run = base + threadIdx.x;
 #pragma unroll
     for (int i = 0; i < R; ++i) {
-      re[i] = im[i] = 0.f;
+      re(i) = im(i) = 0.f;
 #pragma unroll
       for (int v = 0; v < 4; ++v) run[(4 * i + v) * FF_THREADS] = 0.f;
     }
@@ -216,16 +220,16 @@ struct Acc {
     for (int i = 0; i < R; ++i) {
       float* p = run + 4 * i * FF_THREADS;
       float sre = p[0], sim = p[FF_THREADS], cre = p[2 * FF_THREADS], cim = p[3 * FF_THREADS];
-      float y = re[i] - cre, t = sre + y;
+      float y = re(i) - cre, t = sre + y;
       cre = (t - sre) - y;
       sre = t;
-      y = im[i] - cim;
+      y = im(i) - cim;
       t = sim + y;
       cim = (t - sim) - y;
       sim = t;
       p[0] = sre; p[FF_THREADS] = sim; p[2 * FF_THREADS] = cre; p[3 * FF_THREADS] = cim;
-      re[i] = 0.f;
-      im[i] = 0.f;
+      re(i) = 0.f;
+      im(i) = 0.f;
     }
   }
   __device__ __forceinline__ float sre(int i) const { return run[4 * i * FF_THREADS]; }
@@ -271,7 +275,10 @@ ff_kernel(KGridDev kg, BatchDev b, float2* __restrict__ J, int scale_sqrt_w, con
       dl = make_float3((float)(e[0] - (double)dh.x), (float)(e[1] - (double)dh.y), (float)(e[2] - (double)dh.z));
     }
   }
-  // radii r = rb + nrb * i: every warp sees small and large k alike.
+  // radii r = rb R + i: a warp's radii are neighbours, so warps at small k
+  // take the short series for every radius of most elements (the lean loop
+  // below, chosen once per element for the whole warp), and the branches of
+  // the others are taken together more often.
   // The warp's radii as (k 256 / 2 pi hi, lo, k^2, k^3), in shared memory:
   // every lane reads the same entry (a broadcast), once per element and
   // radius, which keeps them out of the registers the element loop needs.
@@ -280,14 +287,34 @@ ff_kernel(KGridDev kg, BatchDev b, float2* __restrict__ J, int scale_sqrt_w, con
   __shared__ float2 ctab[256];
   for (int t = threadIdx.x; t < 256; t += FF_THREADS) ctab[t] = kg.cis_tab[t];
   if (lane < R) {
-    const int r = rb + nrb * lane;
+    const int r = rb * R + lane;
     const bool ok = item < ndt * nrb && r < kg.L;
     const float2 k = ok ? kg.kmag[r] : make_float2(0.f, 0.f);
     const float2 k2 = ok ? kg.kt256[r] : make_float2(0.f, 0.f);
     krad[warp][lane] = make_float4(k2.x, k2.y, k.x * k.x, k.x * k.x * k.x);
   }
+  // the same constants paired for packed FP32: radii (2p, 2p + 1) as
+  // (kt.hi, kt.hi', kt.lo, kt.lo') and (k^2, k^2', k^3, k^3')
+  __shared__ float4 kpair[FF_WARPS][R];
+  if (lane < R / 2) {
+    float v[2][4];
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const int r = rb * R + 2 * lane + h;
+      const bool ok = item < ndt * nrb && r < kg.L;
+      const float2 k = ok ? kg.kmag[r] : make_float2(0.f, 0.f);
+      const float2 k2 = ok ? kg.kt256[r] : make_float2(0.f, 0.f);
+      v[h][0] = k2.x; v[h][1] = k2.y; v[h][2] = k.x * k.x; v[h][3] = k.x * k.x * k.x;
+    }
+    kpair[warp][2 * lane] = make_float4(v[0][0], v[1][0], v[0][1], v[1][1]);
+    kpair[warp][2 * lane + 1] = make_float4(v[0][2], v[1][2], v[0][3], v[1][3]);
+  }
   __syncthreads();
   const float4* kw = krad[warp];
+  const float4* kp = kpair[warp];
+  float kmax2 = 0.f;  // the warp's largest k^2
+#pragma unroll
+  for (int i = 0; i < R; ++i) kmax2 = fmaxf(kmax2, kw[i].z);
   __shared__ float run_sm[4 * R * FF_THREADS];
   Acc<R> acc;
   acc.init(run_sm);
@@ -321,9 +348,26 @@ ff_kernel(KGridDev kg, BatchDev b, float2* __restrict__ J, int scale_sqrt_w, con
           const float4 ml = tile[3 * FF_TILE + e];
           const df sm = cdot2_un(dh, dl, m, make_float3(ml.x, ml.y, ml.z));
           const float kl = ml.w * dnorm;  // k kl bounds k sp: the short series below k kl = 1
-          const float kl2 = kl * kl;
+          const float slim = rcp_fast(kl * kl);  // the short series for k^2 < 1 / kl^2 (inf when kl = 0)
           const float s1 = fmaf(dh.x, e1.x, fmaf(dh.y, e1.y, dh.z * e1.z));
           const float s2 = fmaf(dh.x, e2.x, fmaf(dh.y, e2.y, dh.z * e2.z));
+          if (kmax2 < slim) {
+            // every radius of this thread takes the short series (the same for
+            // all lanes on a tensor grid: unit directions)
+            // two radii per packed FP32 instruction: the same operations,
+            // roundings and results as the scalar loop below
+            const TriPolyShort tp = tri_series_coeffs_short(s1, s2, g);
+            const float2 smh = make_float2(sm.hi, sm.hi), sml = make_float2(sm.lo, sm.lo);
+#pragma unroll
+            for (int p = 0; p < R / 2; ++p) {
+              const float4 kx = ld_shared_f4(kp + 2 * p), ku = ld_shared_f4(kp + 2 * p + 1);
+              const cf2 P = cis_tab_df2(ctab, make_float2(kx.x, kx.y), make_float2(kx.z, kx.w), smh, sml);
+              const cf2 T = tri_series_eval_short2(tp, make_float2(ku.x, ku.y), make_float2(ku.z, ku.w));
+              acc.re2[p] = __ffma2_rn(P.re, T.re, __ffma2_rn(neg2(P.im), T.im, acc.re2[p]));
+              acc.im2[p] = __ffma2_rn(P.re, T.im, __ffma2_rn(P.im, T.re, acc.im2[p]));
+            }
+            continue;
+          }
           const float sp = fmaxf(fmaxf(fabsf(s1), fabsf(s2)), fabsf(s2 - s1));
           const float kthr2 = __fdividef(4.0f, sp * sp);  // the series for (k sp)^2 < 4 (inf when sp = 0)
           const TriPoly tp = tri_series_coeffs(s1, s2, g);
@@ -335,7 +379,7 @@ ff_kernel(KGridDev kg, BatchDev b, float2* __restrict__ J, int scale_sqrt_w, con
             const float2 kt = make_float2(kr.x, kr.y);
             const cf P = cis_tab_df(ctab, kt, sm);  // centroid phase
             cf T;
-            if (kr.z * kl2 < 1.0f) {  // the same for all lanes on a tensor grid (unit directions)
+            if (kr.z < slim) {  // the same for all lanes on a tensor grid (unit directions)
               T = tri_series_eval_short(tp, kr.z, kr.w);
             } else if (kr.z < kthr2) {
               T = tri_series_eval(tp, kr.z, kr.w);  // centroid Taylor series, gamma folded in
@@ -349,8 +393,8 @@ ff_kernel(KGridDev kg, BatchDev b, float2* __restrict__ J, int scale_sqrt_w, con
                                        k * s1, k * s2);
               T = cf{g * v.re, g * v.im};
             }
-            acc.re[i] = fmaf(P.re, T.re, fmaf(-P.im, T.im, acc.re[i]));
-            acc.im[i] = fmaf(P.re, T.im, fmaf(P.im, T.re, acc.im[i]));
+            acc.re(i) = fmaf(P.re, T.re, fmaf(-P.im, T.im, acc.re(i)));
+            acc.im(i) = fmaf(P.re, T.im, fmaf(P.im, T.re, acc.im(i)));
           }
         }
         if (e1 - e0 == FF_CHUNK) acc.flush();
@@ -391,27 +435,30 @@ ff_kernel(KGridDev kg, BatchDev b, float2* __restrict__ J, int scale_sqrt_w, con
                       cz = fmaf(v.x, nr.y, -v.y * nr.x);
           const float perp = fmaf(qd, nr.w, (1.0f - nr.w) * fmaf(cx, cx, fmaf(cy, cy, cz * cz)));
           const float amp = sn * inv_norm * q1.w;                   // area|w * (k'.n)/|k|
+          // two radii per packed FP32 phasor and accumulation (cis_tab_df2)
+          const float2 sch = make_float2(sc.hi, sc.hi), scl = make_float2(sc.lo, sc.lo);
           if (disk) {
             const float rr = q0.w * sqrt_fast(fmaxf(perp, 0.f)) * PI_TURN256;  // rho |k'_perp| / kmag, per 1/256 turn
 #pragma unroll
-            for (int i = 0; i < R; ++i) {
-              const float4 kr = ld_shared_f4(kw + i);
-              const float x = kr.x * rr;
-              const float S = (x < 1e-10f) ? 1.0f : 2.0f * j1x(x);
-              const cf P = cis_tab_df(ctab, make_float2(kr.x, kr.y), sc);
-              const float m = S * amp;
-              acc.re[i] = fmaf(m, P.re, acc.re[i]);
-              acc.im[i] = fmaf(m, P.im, acc.im[i]);
+            for (int p = 0; p < R / 2; ++p) {
+              const float4 kx = ld_shared_f4(kp + 2 * p);
+              const float xa = kx.x * rr, xb = kx.y * rr;
+              const float Sa = (xa < 1e-10f) ? 1.0f : 2.0f * j1x(xa);
+              const float Sb = (xb < 1e-10f) ? 1.0f : 2.0f * j1x(xb);
+              const cf2 P = cis_tab_df2(ctab, make_float2(kx.x, kx.y), make_float2(kx.z, kx.w), sch, scl);
+              const float2 m = make_float2(Sa * amp, Sb * amp);
+              acc.re2[p] = __ffma2_rn(m, P.re, acc.re2[p]);
+              acc.im2[p] = __ffma2_rn(m, P.im, acc.im2[p]);
             }
           } else {
             const float hs = -0.5f * q0.w * q0.w * perp;
 #pragma unroll
-            for (int i = 0; i < R; ++i) {
-              const float4 kr = ld_shared_f4(kw + i);
-              const float m = __expf(hs * kr.z) * amp;
-              const cf P = cis_tab_df(ctab, make_float2(kr.x, kr.y), sc);
-              acc.re[i] = fmaf(m, P.re, acc.re[i]);
-              acc.im[i] = fmaf(m, P.im, acc.im[i]);
+            for (int p = 0; p < R / 2; ++p) {
+              const float4 kx = ld_shared_f4(kp + 2 * p), ku = ld_shared_f4(kp + 2 * p + 1);
+              const float2 m = make_float2(__expf(hs * ku.x) * amp, __expf(hs * ku.y) * amp);
+              const cf2 P = cis_tab_df2(ctab, make_float2(kx.x, kx.y), make_float2(kx.z, kx.w), sch, scl);
+              acc.re2[p] = __ffma2_rn(m, P.re, acc.re2[p]);
+              acc.im2[p] = __ffma2_rn(m, P.im, acc.im2[p]);
             }
           }
         }
@@ -428,7 +475,7 @@ ff_kernel(KGridDev kg, BatchDev b, float2* __restrict__ J, int scale_sqrt_w, con
     float m = 0.f;
 #pragma unroll
     for (int i = 0; i < R; ++i) {
-      const int r = rb + nrb * i;
+      const int r = rb * R + i;
       if (r < kg.L) {
         const int64_t q = (int64_t)r * kg.M + j;
         cf v{acc.sre(i), acc.sim(i)};
@@ -451,7 +498,7 @@ ff_kernel(KGridDev kg, BatchDev b, float2* __restrict__ J, int scale_sqrt_w, con
   float m = 0.f;
 #pragma unroll
   for (int i = 0; i < R; ++i) {
-    const int r = rb + nrb * i;
+    const int r = rb * R + i;
     if (r < kg.L) {
       const int64_t q = (int64_t)r * kg.M + j;
       const double kd = ((double)kw[i].x + (double)kw[i].y) * (6.283185307179586476925 / 256.0);
@@ -476,7 +523,7 @@ __global__ void to_double2_kernel(const float2* __restrict__ J, int64_t n, doubl
 
 }  // namespace
 
-static int radii_per_thread(int L) { return L >= 32 ? 8 : L >= 4 ? 4 : 1; }
+static int radii_per_thread(int L) { return L >= 32 ? 8 : L >= 4 ? 4 : 2; }  // even: radii are paired
 
 int launch_prepare(pi_batch_impl* b, int only_index, cudaStream_t s) {
   std::vector<PrepObj> h(b->n_obj);
@@ -526,7 +573,7 @@ int launch_form_factors(const pi_kgrid_impl* kg, const pi_batch_impl* b, int sca
   switch (R) {
     case 8: ff_kernel<8, false><<<grid, FF_THREADS, 0, s>>>(K, B, J, scale_sqrt_w, nullptr, ra); break;
     case 4: ff_kernel<4, false><<<grid, FF_THREADS, 0, s>>>(K, B, J, scale_sqrt_w, nullptr, ra); break;
-    default: ff_kernel<1, false><<<grid, FF_THREADS, 0, s>>>(K, B, J, scale_sqrt_w, nullptr, ra); break;
+    default: ff_kernel<2, false><<<grid, FF_THREADS, 0, s>>>(K, B, J, scale_sqrt_w, nullptr, ra); break;
   }
   PI_LAUNCHED("ff_kernel");
   return PI_OK;
@@ -544,7 +591,7 @@ const void* ff_serve_fn(const pi_kgrid_impl* kg) {
   switch (radii_per_thread(kg->dev.L)) {
     case 8: return reinterpret_cast<const void*>(ff_kernel<8, true>);
     case 4: return reinterpret_cast<const void*>(ff_kernel<4, true>);
-    default: return reinterpret_cast<const void*>(ff_kernel<1, true>);
+    default: return reinterpret_cast<const void*>(ff_kernel<2, true>);
   }
 }
 

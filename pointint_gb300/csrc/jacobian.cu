@@ -81,6 +81,7 @@ struct JacThread {
   float3 dh, dl;
   float inv_norm, dnorm;
   df k;
+  float2 kt;  // |k| in 1/256 turns per unit length (double-float), for the table phasors
 };
 
 __device__ __forceinline__ JacThread jac_thread(const KGridDev& kg) {
@@ -94,6 +95,7 @@ __device__ __forceinline__ JacThread jac_thread(const KGridDev& kg) {
   t.dh = t.dl = make_float3(0.f, 0.f, 0.f);
   t.inv_norm = t.dnorm = 0.f;
   t.k = df{0.f, 0.f};
+  t.kt = make_float2(0.f, 0.f);
   if (t.active) {
     const float4 h = kg.dir_hi[t.j], l = kg.dir_lo[t.j];
     t.dh = make_float3(h.x, h.y, h.z);
@@ -102,8 +104,16 @@ __device__ __forceinline__ JacThread jac_thread(const KGridDev& kg) {
     t.dnorm = l.w;
     const float2 km = kg.kmag[t.r];
     t.k = df{km.x, km.y};
+    t.kt = kg.kt256[t.r];
   }
   return t;
+}
+
+// The 256-entry phasor table of cis_tab_df in shared memory; every thread of
+// the CTA calls this before its first use (it ends in __syncthreads).
+__device__ __forceinline__ void stage_cis_tab(const KGridDev& kg, float2* ctab) {
+  for (int i = threadIdx.x; i < 256; i += blockDim.x) ctab[i] = kg.cis_tab[i];
+  __syncthreads();
 }
 
 // e^{ik.o} sqrt|w| for this thread's node (0 at k = 0, where A = 0 by definition).
@@ -124,14 +134,15 @@ struct TriNode {
 };
 
 // ml: the centroid's low word, and in .w the longest edge (the series-length bound).
-__device__ __forceinline__ TriNode tri_node(const JacThread& t, float3 m, float4 ml, float3 e1, float3 e2, float3 S) {
+__device__ __forceinline__ TriNode tri_node(const JacThread& t, const float2* ctab, float3 m, float4 ml, float3 e1,
+                                            float3 e2, float3 S) {
   TriNode o;
   const df sm = cdot2(t.dh, t.dl, m, make_float3(ml.x, ml.y, ml.z)), d1 = cdot(t.dh, t.dl, e1),
            d2 = cdot(t.dh, t.dl, e2);
   const float sp = fmaxf(fmaxf(fabsf(d1.hi), fabsf(d2.hi)), fabsf(d2.hi - d1.hi));
   const float al = t.k.hi * d1.hi, be = t.k.hi * d2.hi;
   if (t.k.hi * sp < 2.0f) {
-    const cf P = cis(df_mul_un(t.k, sm));
+    const cf P = cis_tab_df(ctab, t.kt, sm);
     // the lanes of a warp share the radius and the element: a uniform branch
     if (t.k.hi * t.dnorm * ml.w < 1.0f)
       o.d = tri_series_der<8>(P, al, be);
@@ -140,7 +151,7 @@ __device__ __forceinline__ TriNode tri_node(const JacThread& t, float3 m, float4
   } else {
     const df sa = df_add(sm, df_div3(df_add(d1, d2)) * -1.0f);
     const df sb = df_add(sa, d1), sc = df_add(sa, d2);
-    o.d = tri_generic_der(cis(df_mul_un(t.k, sa)), cis(df_mul_un(t.k, sb)), cis(df_mul_un(t.k, sc)), al, be);
+    o.d = tri_generic_der(cis_tab_df(ctab, t.kt, sa), cis_tab_df(ctab, t.kt, sb), cis_tab_df(ctab, t.kt, sc), al, be);
   }
   o.gam = (t.dh.x * S.x + t.dh.y * S.y + t.dh.z * S.z) * t.inv_norm;
   const float3 kh = make_float3(t.dh.x * t.inv_norm, t.dh.y * t.inv_norm, t.dh.z * t.inv_norm);
@@ -163,7 +174,9 @@ jac_affine_tri_kernel(KGridDev kg, BatchDev b, const JacObj* __restrict__ jobs, 
   const ObjDev od = b.objs[jo.obj];
   const JacThread t = jac_thread(kg);
   __shared__ float4 tile[7 * JAC_TILE];
-  kcf A, MF[9], W[3];
+  __shared__ float2 ctab[256];
+  stage_cis_tab(kg, ctab);
+  kcf A, NF[3], W[3];
   const float4* pool = b.tri_pool + 3 * od.elem_off;
   const float4* pool_lo = b.tri_lo + od.elem_off;
   const TriSrcJ* src = reinterpret_cast<const TriSrcJ*>(jo.src);
@@ -174,49 +187,50 @@ jac_affine_tri_kernel(KGridDev kg, BatchDev b, const JacObj* __restrict__ jobs, 
       tile[6 * e] = pool[3 * (int64_t)(base + e)];
       tile[6 * e + 1] = pool[3 * (int64_t)(base + e) + 1];
       tile[6 * e + 2] = pool[3 * (int64_t)(base + e) + 2];
-      const TriSrcJ& s = src[base + e];  // reference positions x0 of the three vertices
-      tile[6 * e + 3] = make_float4((float)s.a[0], (float)s.a[1], (float)s.a[2], 0.f);
-      tile[6 * e + 4] = make_float4((float)(s.a[0] + s.e1[0]), (float)(s.a[1] + s.e1[1]), (float)(s.a[2] + s.e1[2]), 0.f);
-      tile[6 * e + 5] = make_float4((float)(s.a[0] + s.e2[0]), (float)(s.a[1] + s.e2[1]), (float)(s.a[2] + s.e2[2]), 0.f);
+      // the reference vertex a0 and edges E1, E2; in .w the reference
+      // doubled area vector N0 = E1 x E2
+      const TriSrcJ& s = src[base + e];
+      const double n0x = s.e1[1] * s.e2[2] - s.e1[2] * s.e2[1], n0y = s.e1[2] * s.e2[0] - s.e1[0] * s.e2[2],
+                   n0z = s.e1[0] * s.e2[1] - s.e1[1] * s.e2[0];
+      tile[6 * e + 3] = make_float4((float)s.a[0], (float)s.a[1], (float)s.a[2], (float)n0x);
+      tile[6 * e + 4] = make_float4((float)s.e1[0], (float)s.e1[1], (float)s.e1[2], (float)n0y);
+      tile[6 * e + 5] = make_float4((float)s.e2[0], (float)s.e2[1], (float)s.e2[2], (float)n0z);
       tile[6 * JAC_TILE + e] = pool_lo[base + e];  // centroid low word
     }
     __syncthreads();
     if (!t.active) continue;
     for (int e = 0; e < cnt; ++e) {
       const float4 q0 = tile[6 * e], q1 = tile[6 * e + 1], q2 = tile[6 * e + 2], ql = tile[6 * JAC_TILE + e];
-      const float3 x0[3] = {make_float3(tile[6 * e + 3].x, tile[6 * e + 3].y, tile[6 * e + 3].z),
-                            make_float3(tile[6 * e + 4].x, tile[6 * e + 4].y, tile[6 * e + 4].z),
-                            make_float3(tile[6 * e + 5].x, tile[6 * e + 5].y, tile[6 * e + 5].z)};
-      const TriNode o = tri_node(t, make_float3(q0.x, q0.y, q0.z), ql, make_float3(q1.x, q1.y, q1.z),
+      const float3 a0 = make_float3(tile[6 * e + 3].x, tile[6 * e + 3].y, tile[6 * e + 3].z),
+                   E1 = make_float3(tile[6 * e + 4].x, tile[6 * e + 4].y, tile[6 * e + 4].z),
+                   E2 = make_float3(tile[6 * e + 5].x, tile[6 * e + 5].y, tile[6 * e + 5].z);
+      const TriNode o = tri_node(t, ctab, make_float3(q0.x, q0.y, q0.z), ql, make_float3(q1.x, q1.y, q1.z),
                                  make_float3(q2.x, q2.y, q2.z), make_float3(q0.w, q1.w, q2.w));
       A.fma_add(o.d.F, -2.0f * o.gam);
-      const cf Ds[3] = {o.d.Da, o.d.Db, o.d.Dc};
-#pragma unroll
-      for (int r = 0; r < 3; ++r)
-#pragma unroll
-        for (int c = 0; c < 3; ++c) {
-          const float U = comp(o.c[0], r) * comp(x0[0], c) + comp(o.c[1], r) * comp(x0[1], c) +
-                          comp(o.c[2], r) * comp(x0[2], c);
-          MF[3 * r + c].fma_add(o.d.F, U);
-        }
+      // sum_s grad_s(gamma) x0_s^T = (khat / 2) x (A [N0]_x) with [N0]_x v = v x N0
+      // (the sum over s of the gamma gradients is zero, so the vertex
+      // positions drop out): only F N0 is accumulated; khat x and A are
+      // applied once per node below
+      NF[0].fma_add(o.d.F, tile[6 * e + 3].w);
+      NF[1].fma_add(o.d.F, tile[6 * e + 4].w);
+      NF[2].fma_add(o.d.F, tile[6 * e + 5].w);
+      // W_c += gamma sum_s D_s x0_s[c] with x0 = (a0, a0 + E1, a0 + E2) and
+      // D_a + D_b + D_c = i F: gamma (i F a0[c] + D_b E1[c] + D_c E2[c])
+      const cf gF = cscale(o.d.F, o.gam), gB = cscale(o.d.Db, o.gam), gC = cscale(o.d.Dc, o.gam);
 #pragma unroll
       for (int c = 0; c < 3; ++c) {
-        const float w0 = o.gam * comp(x0[0], c), w1 = o.gam * comp(x0[1], c), w2 = o.gam * comp(x0[2], c);
-        W[c].add(Ds[0].re * w0 + Ds[1].re * w1 + Ds[2].re * w2, Ds[0].im * w0 + Ds[1].im * w1 + Ds[2].im * w2);
+        const float x = comp(a0, c), y = comp(E1, c), z = comp(E2, c);
+        W[c].add(fmaf(-gF.im, x, fmaf(gB.re, y, gC.re * z)), fmaf(gF.re, x, fmaf(gB.im, y, gC.im * z)));
       }
       if ((e & 15) == 15) {
         A.flush();
 #pragma unroll
-        for (int a = 0; a < 9; ++a) MF[a].flush();
-#pragma unroll
-        for (int a = 0; a < 3; ++a) W[a].flush();
+        for (int a = 0; a < 3; ++a) { NF[a].flush(); W[a].flush(); }
       }
     }
     A.flush();
 #pragma unroll
-    for (int a = 0; a < 9; ++a) MF[a].flush();
-#pragma unroll
-    for (int a = 0; a < 3; ++a) W[a].flush();
+    for (int a = 0; a < 3; ++a) { NF[a].flush(); W[a].flush(); }
   }
   if (!t.active) return;
   const int64_t q = (int64_t)t.r * kg.M + t.j;
@@ -229,11 +243,32 @@ jac_affine_tri_kernel(KGridDev kg, BatchDev b, const JacObj* __restrict__ jobs, 
     const float kr = k * comp(t.dh, r);
     out[(int64_t)r * kg.Q] = make_float2(-kr * a.im, kr * a.re);
   }
+  // MF[r][c] = sum_e F_e sum_s grad_s(gamma)_r x0_s[c] = ((khat / 2) x (A (e_c x N~)))_r, N~ = sum_e F_e N0_e
+  const double* Am = jo.dofs + 3;  // A row-major
+  const cf Nt[3] = {NF[0].value(), NF[1].value(), NF[2].value()};
+  const float3 kh = make_float3(0.5f * t.dh.x * t.inv_norm, 0.5f * t.dh.y * t.inv_norm, 0.5f * t.dh.z * t.inv_norm);
+  cf MF[9];
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    cf v[3];  // e_c x N~
+    v[c] = cf{0.f, 0.f};
+    v[(c + 1) % 3] = cf{-Nt[(c + 2) % 3].re, -Nt[(c + 2) % 3].im};
+    v[(c + 2) % 3] = Nt[(c + 1) % 3];
+    cf m[3];  // A v
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      const float a0 = (float)Am[3 * i], a1 = (float)Am[3 * i + 1], a2 = (float)Am[3 * i + 2];
+      m[i] = cf{fmaf(a0, v[0].re, fmaf(a1, v[1].re, a2 * v[2].re)), fmaf(a0, v[0].im, fmaf(a1, v[1].im, a2 * v[2].im))};
+    }
+    MF[c] = cf{comp(kh, 1) * m[2].re - comp(kh, 2) * m[1].re, comp(kh, 1) * m[2].im - comp(kh, 2) * m[1].im};
+    MF[3 + c] = cf{comp(kh, 2) * m[0].re - comp(kh, 0) * m[2].re, comp(kh, 2) * m[0].im - comp(kh, 0) * m[2].im};
+    MF[6 + c] = cf{comp(kh, 0) * m[1].re - comp(kh, 1) * m[0].re, comp(kh, 0) * m[1].im - comp(kh, 1) * m[0].im};
+  }
 #pragma unroll
   for (int r = 0; r < 3; ++r)
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
-      const cf mf = MF[3 * r + c].value(), w = W[c].value();
+      const cf mf = MF[3 * r + c], w = W[c].value();
       const float kd = k * comp(t.dh, r);
       const cf v = cmul(cf{-2.0f * (mf.re + kd * w.re), -2.0f * (mf.im + kd * w.im)}, sc);
       out[(int64_t)(3 + 3 * r + c) * kg.Q] = make_float2(v.re, v.im);
@@ -248,6 +283,8 @@ jac_affine_surf_kernel(KGridDev kg, BatchDev b, const JacObj* __restrict__ jobs,
   const JacThread t = jac_thread(kg);
   const bool disk = od.type == PI_GEOM_DISK;
   __shared__ float4 tile[6 * JAC_TILE];
+  __shared__ float2 ctab[256];
+  stage_cis_tab(kg, ctab);
   // v = A^T dir (k' = |k| v), qd = |v|^2
   const float* Af = od.A;
   const float3 v = make_float3(Af[0] * t.dh.x + Af[3] * t.dh.y + Af[6] * t.dh.z,
@@ -285,7 +322,7 @@ jac_affine_surf_kernel(KGridDev kg, BatchDev b, const JacObj* __restrict__ jobs,
                   cz = fmaf(v.x, nr.y, -v.y * nr.x);
       const float perp = fmaxf(fmaf(qd, nr.w, (1.0f - nr.w) * fmaf(cx, cx, fmaf(cy, cy, cz * cz))), 0.f);
       const float amp = sn * t.inv_norm;
-      const cf P = cis(df_mul_un(t.k, sc));
+      const cf P = cis_tab_df(ctab, t.kt, sc);
       float S, Sr;
       if (disk) {
         const float x = k * q0.w * sqrt_fast(perp);
@@ -345,6 +382,8 @@ jac_mesh_kernel(KGridDev kg, BatchDev b, const JacObj* __restrict__ jobs, const 
   const JacObj jo = jobs[blockIdx.y];
   const ObjDev od = b.objs[jo.obj];
   const JacThread t = jac_thread(kg);
+  __shared__ float2 ctab[256];
+  stage_cis_tab(kg, ctab);
   if (!t.active) return;
   const int64_t q = (int64_t)t.r * kg.M + t.j;
   const cf scl = jac_out_scale(t, kg, od, q);
@@ -357,7 +396,7 @@ jac_mesh_kernel(KGridDev kg, BatchDev b, const JacObj* __restrict__ jobs, const 
       const int slot = (int)(te - 3 * tri);
       const float4 q0 = b.tri_pool[3 * tri], q1 = b.tri_pool[3 * tri + 1], q2 = b.tri_pool[3 * tri + 2];
       const float4 ql = b.tri_lo[tri];
-      const TriNode o = tri_node(t, make_float3(q0.x, q0.y, q0.z), ql, make_float3(q1.x, q1.y, q1.z),
+      const TriNode o = tri_node(t, ctab, make_float3(q0.x, q0.y, q0.z), ql, make_float3(q1.x, q1.y, q1.z),
                                  make_float3(q2.x, q2.y, q2.z), make_float3(q0.w, q1.w, q2.w));
       const cf D = slot == 0 ? o.d.Da : (slot == 1 ? o.d.Db : o.d.Dc);
       const float3 cs = o.c[slot];

@@ -180,8 +180,11 @@ __device__ __forceinline__ TriDer tri_generic_der(cf Pa, cf Pb, cf Pc, float al,
 // a kernel whose hot radius loop inlines this rarely taken path as well as the
 // series outgrows the instruction cache (the loop then stalls on instruction
 // fetch), while the call costs little on the few nodes that take it.
-static __device__ __noinline__ TriDer tri_generic_der_at(df k, df sa, df sb, df sc, float al, float be) {
-  return tri_generic_der(cis(df_mul_un(k, sa)), cis(df_mul_un(k, sb)), cis(df_mul_un(k, sc)), al, be);
+// The vertex phasors come from the phasor table (cis_tab_df): tab is the
+// 256-entry table, kt the radius in 1/256 turns per unit length.
+static __device__ __noinline__ TriDer tri_generic_der_at(const float2* tab, float2 kt, df sa, df sb, df sc, float al,
+                                                         float be) {
+  return tri_generic_der(cis_tab_df(tab, kt, sa), cis_tab_df(tab, kt, sb), cis_tab_df(tab, kt, sc), al, be);
 }
 
 }  // namespace pi
