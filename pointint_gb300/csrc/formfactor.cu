@@ -236,7 +236,12 @@ struct Acc {
   __device__ __forceinline__ float sim(int i) const { return run[(4 * i + 1) * FF_THREADS]; }
 };
 
-// SERVE: blockIdx.y indexes `evals` (serving evaluations: optional rotation of
+// The grid is (CTAs per object) x (objects or evaluations); the CTAs are
+// taken in the order the hardware dispatches them (x fastest, then y) and
+// re-mapped so that the object slot varies fastest and the CTA index within
+// the object slowest: every object's first CTAs (its largest-k radial block,
+// below) run before any object's later ones.
+// SERVE: the object slot indexes `evals` (serving evaluations: optional rotation of
 // the k directions, local-frame direction-major output, row maximum);
 // otherwise it indexes the batch's objects (largest first) and J is written
 // q-major with the origin phase.
@@ -244,7 +249,9 @@ template <int R, bool SERVE>
 __global__ void __launch_bounds__(FF_THREADS, 5)
 ff_kernel(KGridDev kg, BatchDev b, float2* __restrict__ J, int scale_sqrt_w, const EvalDev* __restrict__ evals,
           unsigned* __restrict__ row_amax) {
-  const int oi = SERVE ? evals[blockIdx.y].obj : b.order[blockIdx.y];
+  const unsigned lin = blockIdx.y * gridDim.x + blockIdx.x;
+  const int slot = (int)(lin % gridDim.y), cta = (int)(lin / gridDim.y);
+  const int oi = SERVE ? evals[slot].obj : b.order[slot];
   const ObjDev od = b.objs[oi];
   const int nrb = (kg.L + R - 1) / R;
   const int ndt = (kg.M + 31) / 32;
@@ -252,8 +259,14 @@ ff_kernel(KGridDev kg, BatchDev b, float2* __restrict__ J, int scale_sqrt_w, con
   // Warps of a CTA take neighbouring direction blocks at the same radial
   // block: they see the same radii, so they take the large-spread branch at
   // the same points of the element loop and reach the tile barriers together.
-  const int item = blockIdx.x * FF_WARPS + warp;
-  const int rb = item / ndt, dt = item - rb * ndt;
+  // Radial blocks run in descending order of k: on a grid of ascending radii
+  // the blocks of large k, whose elements take the long branches, start
+  // first (for all objects, by the re-mapping above) and the launch ends on
+  // light blocks (with neighbouring radii per warp the blocks differ
+  // several-fold in cost).
+  const int item = cta * FF_WARPS + warp;
+  const int ib = item / ndt, dt = item - ib * ndt;
+  const int rb = ib < nrb ? nrb - 1 - ib : 0;
   const int j = dt * 32 + lane;
   const bool active = item < ndt * nrb && j < kg.M;
 
@@ -263,10 +276,10 @@ ff_kernel(KGridDev kg, BatchDev b, float2* __restrict__ J, int scale_sqrt_w, con
     float4 h = kg.dir_hi[j], l = kg.dir_lo[j];
     dh = make_float3(h.x, h.y, h.z); dl = make_float3(l.x, l.y, l.z);
     inv_norm = h.w; dnorm = l.w;
-    if (SERVE && evals[blockIdx.y].rotate) {
+    if (SERVE && evals[slot].rotate) {
       // rotated object: its form factor at k is the unrotated one's at R^T k
       // (|R^T k| = |k|); the direction is turned in FP64 and re-split.
-      const double* Rm = evals[blockIdx.y].R;
+      const double* Rm = evals[slot].R;
       const double d0 = (double)h.x + (double)l.x, d1 = (double)h.y + (double)l.y, d2 = (double)h.z + (double)l.z;
       double e[3];
 #pragma unroll
@@ -369,7 +382,7 @@ ff_kernel(KGridDev kg, BatchDev b, float2* __restrict__ J, int scale_sqrt_w, con
             continue;
           }
           const float sp = fmaxf(fmaxf(fabsf(s1), fabsf(s2)), fabsf(s2 - s1));
-          const float kthr2 = __fdividef(4.0f, sp * sp);  // the series for (k sp)^2 < 4 (inf when sp = 0)
+          const float kthr2 = __fdividef(9.0f, sp * sp);  // the series for (k sp)^2 < 9 (inf when sp = 0)
           const TriPoly tp = tri_series_coeffs(s1, s2, g);
           // vertex phases relative to the centroid (a = m - (e1 + e2)/3, b = a + e1, c = a + e2)
           const float da = -(s1 + s2) * (1.0f / 3.0f), db = da + s1, dc = da + s2;
@@ -471,7 +484,7 @@ ff_kernel(KGridDev kg, BatchDev b, float2* __restrict__ J, int scale_sqrt_w, con
   if (!active) return;
   acc.flush();
   if (SERVE) {
-    const EvalDev& ev = evals[blockIdx.y];
+    const EvalDev& ev = evals[slot];
     float m = 0.f;
 #pragma unroll
     for (int i = 0; i < R; ++i) {

@@ -5,7 +5,7 @@ For centred vertex phases x = k (d_a, d_b, d_c) (d_a + d_b + d_c = 0) the
 triangle's e[x_a, x_b, x_c] = sum_m i^{m+2} h_m(x) / (m+2)!, and the vertex
 derivative pieces e[x_a, x_b, x_b, x_c] = sum_m i^{m+3} h_m(x, x_b) / (m+3)!,
 with h_m the complete homogeneous symmetric polynomials.  The kernels take
-  * the form factor series to h_12 for k sp < 2 (sp = the largest |k.e|),
+  * the form factor series to h_13 for k sp < 3 (sp = the largest |k.e|),
     and to h_7 (a[0..3], b[0..2]) where k |e|max < 1 (|e|max = longest edge);
   * the derivative series to h_12 for k sp < 2, and to h_8 where k |e|max < 1.
 Each cut must stay well below FP32 rounding of the leading term (6e-8)."""
@@ -38,12 +38,12 @@ def centred(e1, e2, d):
 
 
 def hseries(dv):
-    """h_0..h_12 of the centred dots: the recurrence the kernels use."""
+    """h_0..h_13 of the centred dots: the recurrence the kernels use."""
     da, db, dc = dv
     mu = 0.5 * (da * da + db * db + dc * dc)
     nu = da * db * dc
     h = [1.0, 0.0, mu, nu]
-    for m in range(4, 13):
+    for m in range(4, 14):
         h.append(mu * h[m - 2] + nu * h[m - 3])
     return h
 
@@ -84,23 +84,21 @@ def exact_Db(dv, k):
 
 @pytest.mark.parametrize("seed", [0, 1])
 def test_series_cuts_against_exact_divided_differences(seed):
-    worst = {"F12": 0.0, "F7": 0.0, "Db12": 0.0, "Db8": 0.0}
+    worst = {"F13": 0.0, "F7": 0.0, "Db12": 0.0, "Db8": 0.0}
     rng = np.random.default_rng(100 + seed)
     for e1, e2, d in random_cases(150, seed):
         dv, sp, lmax = centred(e1, e2, d)
         if min(abs(dv[0] - dv[1]), abs(dv[1] - dv[2]), abs(dv[0] - dv[2])) < 1e-6 * sp:
             continue  # near-coincident nodes: the exact quotient form loses digits
-        k_full = 2.0 / sp * rng.uniform(0.3, 1.0)  # k sp up to the series threshold 2
+        u = rng.uniform(0.3, 1.0)
+        k_f = 3.0 / sp * u  # k sp up to the form factor series' threshold 3
+        k_d = 2.0 / sp * u  # k sp up to the derivative series' threshold 2
         k_short = 1.0 / lmax * rng.uniform(0.3, 1.0)  # k |e|max up to the short-series bound 1
-        for k, top_f, top_d, tag in ((k_full, 12, 12, "12"), (k_short, 7, 8, "short")):
-            ef = abs(series_F(dv, k, top_f) - exact_F(dv, k)) / 0.5  # leading term i^2 / 2!
-            ed = abs(series_Db(dv, k, top_d) - exact_Db(dv, k)) * 6.0  # leading term i^3 / 3!
-            if tag == "12":
-                worst["F12"] = max(worst["F12"], ef)
-                worst["Db12"] = max(worst["Db12"], ed)
-            else:
-                worst["F7"] = max(worst["F7"], ef)
-                worst["Db8"] = max(worst["Db8"], ed)
+        # leading terms: i^2 / 2! for F, i^3 / 3! for D_b
+        worst["F13"] = max(worst["F13"], abs(series_F(dv, k_f, 13) - exact_F(dv, k_f)) / 0.5)
+        worst["Db12"] = max(worst["Db12"], abs(series_Db(dv, k_d, 12) - exact_Db(dv, k_d)) * 6.0)
+        worst["F7"] = max(worst["F7"], abs(series_F(dv, k_short, 7) - exact_F(dv, k_short)) / 0.5)
+        worst["Db8"] = max(worst["Db8"], abs(series_Db(dv, k_short, 8) - exact_Db(dv, k_short)) * 6.0)
     print("\nseries truncation, worst relative to the leading term:",
           {k: f"{v:.2e}" for k, v in worst.items()})
     for key, v in worst.items():
