@@ -330,8 +330,12 @@ def run_gb300(args):
                                     f"reference algorithm's count, x {evals_step:.4e} evaluations",
                 "peak_source": f"nominal FP32: {FP32_FLOPS_PER_SM_PER_CLK} flops/clk/SM x {n_sm} SMs x {clk_max} MHz "
                                "(MEASURED_PEAKS.json holds HBM and bf16 tensor peaks only)",
-                "binding": "instruction issue of the FP32 pipe: the kernel uses no MUFU (SFU) instructions; its "
-                           "sine/cosine are a phasor table and polynomials",
+                "binding": "FP32 issue and FMA pipe: no MUFU (SFU) instructions (sine/cosine are a phasor table "
+                           "and polynomials); the short-series loop runs two radii per packed FP32 instruction, which "
+                           "holds the FMA pipe two cycles, so the FMA pipe (math-pipe throttle, the second stall) and "
+                           "the issue slots bind together",
+                "pipes_from_capture": {"fma_pipe_active": FF_FMA_PIPE_ACTIVE, "issue_active": FF_ISSUE_ACTIVE,
+                                       "source": "ncu --set full of the same kernel on 32 of the 256 objects"},
                 "issue": {"thread_instructions_per_evaluation": FF_THREAD_INSTR_PER_EVAL,
                           "achieved": issue_achieved, "peak": issue_peak, "unit": "G warp-instructions/s",
                           "frac": issue_achieved / issue_peak,
@@ -371,17 +375,22 @@ def run_gb300(args):
 
 
 # DRAM bytes (read + write) of one full-size ff_kernel launch.  Reads: captured
-# with ncu on 32 of the 256 objects (82,112 triangles: 5.69 MB with the
+# with ncu on 32 of the 256 objects (82,112 triangles: 5.93 MB with the
 # centroid low words) and scaled by
 # the triangle count (656,896 / 82,112), since element reads grow with the
 # elements.  Writes: that capture's J (19.7 MB) stayed in L2, but the full
 # J (256 x 76,928 complex64 = 157.5 MB) exceeds the 129 MB L2 and is counted
 # as written once.
-FF_TRAFFIC_BYTES_PER_LAUNCH = 5.69e6 * 656896 / 82112 + 256 * 76928 * 8
+FF_TRAFFIC_BYTES_PER_LAUNCH = 5.93e6 * 656896 / 82112 + 256 * 76928 * 8
 # Thread instructions per triangle x k evaluation of ff_kernel, from its ncu
-# capture on 32 of the 256 objects (smsp__inst_executed.sum 1.213e10 x 32 /
-# 6.317e9 evaluations).
-FF_THREAD_INSTR_PER_EVAL = 61.5
+# capture on 32 of the 256 objects (smsp__inst_executed.sum 9.336e9 x 32 /
+# 6.317e9 evaluations; packed FP32 instructions count once).
+FF_THREAD_INSTR_PER_EVAL = 47.3
+# The same capture's FMA-pipe busy share (sm__pipe_fma_cycles_active, 62.4%
+# of active cycles, packed FP32 instructions holding the pipe two cycles) and
+# issue-slot share (smsp__issue_active, 73.3%).
+FF_FMA_PIPE_ACTIVE = 0.624
+FF_ISSUE_ACTIVE = 0.733
 
 
 def _pcts(ms):
