@@ -62,7 +62,7 @@ def parse():
     p.add_argument("--objects", type=int, default=256,
                    help="object count of the matrix workload (256 = the benchmark; smaller only for profiling)")
     p.add_argument("--profile-case", default=None,
-                   choices=["contract", "adjoint", "surfel_adjoint", "jacobian", "serve"],
+                   choices=["contract", "adjoint", "surfel_forward", "surfel_adjoint", "jacobian", "serve"],
                    help="run one kernel family's workload a few times (for ncu captures) instead of the benchmark")
     return p.parse_args()
 
@@ -798,7 +798,8 @@ def profile_case(name: str):
     kernels that the benchmark line does not time on their own:
       contract        FP32 / TF32x3 / BF16x3 / FP16x3 contractions of the 256-object J
       adjoint         dV/dtheta of the 256-object matrix (W = 1): adj_tri_kernel + chain
-      surfel_adjoint  per-disk position / normal gradients, 8 objects x 50,000 disks
+      surfel_forward  volume matrix of 8 objects x 50,000 disks (form factors + contraction)
+      surfel_adjoint  the same forward plus per-disk position / normal gradients
       jacobian        DoF Jacobian of the 256-object matrix (3,072 rows)
       serve           the 256-object scene re-queried under translations (20 queries)"""
     import torch
@@ -850,7 +851,7 @@ def profile_case(name: str):
             c = c0.clone().requires_grad_(True)
             nn = n0.clone().requires_grad_(True)
             scene.volume_matrix_of_surfels(c, nn).sum().backward()
-        out["ms"] = timed(fwd_bwd)
+        out["ms"] = timed(fwd_bwd if name == "surfel_adjoint" else lambda: scene.volume_matrix_of_surfels(c0, n0))
     out["workload"] = meta["workload"]
     print(json.dumps(out))
 

@@ -157,7 +157,7 @@ __device__ __forceinline__ void stage_tile(AdjStage& st, const KGridDev& kg, con
 //   dA/dM  = e^{ik.c} (k.n')/|k| (dS/dr)/(2r) k k^T
 // Disk S = area 2 J1(rho r)/(rho r), (dS/dr)/r = -2 area rho^2 J2(x)/x^2;
 // Gaussian S = w exp(-sigma^2 r^2/2), (dS/dr)/r = -sigma^2 S.
-__global__ void __launch_bounds__(ADJ_THREADS, 4)
+__global__ void __launch_bounds__(ADJ_THREADS)
 adj_surf_kernel(KGridDev kg, BatchDev b, const AdjWork* __restrict__ work, const float2* __restrict__ Bw,
                 float* __restrict__ out) {
   __shared__ AdjStage st;

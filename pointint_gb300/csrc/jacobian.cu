@@ -19,7 +19,8 @@
 //
 //  * AffineDoF triangles (x = A x0 + t): dA/dt_r = i k_r A; dA/dA_rc =
 //    sum_e sum_s (df_e/dv_s)_r x0_{s,c} with df/dv_s = -2 (c_s F + gamma k d D_s),
-//    so each thread accumulates sum_e F U_e (U_rc = sum_s c_{s,r} x0_{s,c}) and
+//    so each thread accumulates sum_e F N0_e (from which sum_e F U_e,
+//    U_rc = sum_s c_{s,r} x0_{s,c}, follows per node) and
 //    sum_e gamma sum_s D_s x0_s.
 //  * AffineDoF disks / Gaussians (c = A c0 + t, n' = A n0, M = A A^T):
 //    dA/dA_rc = i k d_r Z_c + khat_r N_c + k^2 d_r (A^T d)_c Y with
@@ -27,9 +28,10 @@
 //  * TriangleMeshDoF: dA/dv_p = sum over the triangles at vertex p of
 //    df_e/dv_p (a gather over the batch's vertex adjacency, no atomics).
 //
-// Thread layout as ff_kernel with one radius per thread: a warp owns 32
-// directions at one radius; the origin phase e^{ik.o} and sqrt|w| are applied
-// once per output.
+// Thread layouts: the affine-triangle kernel as ff_kernel (a warp owns 32
+// directions x JAC_R neighbouring radii); the others one radius per thread (a
+// warp owns 32 directions at one radius).  The origin phase e^{ik.o} and
+// sqrt|w| are applied once per output.
 #include <cuda_runtime.h>
 #include <algorithm>
 #include <cstdint>
@@ -63,7 +65,6 @@ struct SurfSrcJ { double c[3], n[3], p0, p1; };
 // FP32 sum with chunked partials and a compensated running total (complex).
 struct kcf {
   float pr = 0.f, pi = 0.f, sr = 0.f, si = 0.f, cr = 0.f, ci = 0.f;
-  __device__ __forceinline__ void add(float re, float im) { pr += re; pi += im; }
   __device__ __forceinline__ void fma_add(cf a, float s) { pr = fmaf(a.re, s, pr); pi = fmaf(a.im, s, pi); }
   __device__ __forceinline__ void flush() {
     float y = pr - cr, t = sr + y;
@@ -168,15 +169,76 @@ __device__ __forceinline__ TriNode tri_node(const JacThread& t, const float2* ct
 __device__ __forceinline__ float comp(float3 v, int i) { return i == 0 ? v.x : (i == 1 ? v.y : v.z); }
 
 // ---- AffineDoF triangles -------------------------------------------------------------
-__global__ void __launch_bounds__(JAC_THREADS)
+// A thread owns one direction and JAC_R neighbouring radii (the warp 32
+// directions, the CTA 4 neighbouring direction blocks of one radial block).
+// Per element and direction the small-spread series of F, D_b and D_c are
+// formed once as polynomials in k (tri_der_coeffs), so a radius costs a table
+// phasor, the Horner chains (cut after h_8 where k |e|max < 1, a test that is
+// the same for the whole warp on a tensor grid) and three complex products.
+// Radial blocks run heavy-first and the CTA order is re-mapped so that every
+// object's heavy blocks start first, as in ff_kernel.  Per radius and node
+// seven complex sums, chunked in FP32 and Kahan-compensated in shared memory:
+//   A  += -2 gamma F                                   (translations: i k d A)
+//   NF += F N0,  N0 = E1 x E2 (reference edges)        (see MF below)
+//   W  += gamma (i F a0 + D_b E1 + D_c E2)             (sum_s D_s x0_s, D_a + D_b + D_c = i F)
+constexpr int JAC_R = 2;
+constexpr int JAC_NSUM = 14;  // floats per radius: A, NF[3], W[3] (complex)
+
+template <int R>
+__global__ void __launch_bounds__(JAC_THREADS, 4)
 jac_affine_tri_kernel(KGridDev kg, BatchDev b, const JacObj* __restrict__ jobs, float2* __restrict__ G) {
-  const JacObj jo = jobs[blockIdx.y];
+  const unsigned lin = blockIdx.y * gridDim.x + blockIdx.x;
+  const int slot = (int)(lin % gridDim.y), cta = (int)(lin / gridDim.y);
+  const JacObj jo = jobs[slot];
   const ObjDev od = b.objs[jo.obj];
-  const JacThread t = jac_thread(kg);
+  const int nrb = (kg.L + R - 1) / R, ndt = (kg.M + 31) / 32;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int item = cta * JAC_WARPS + warp;
+  const int ib = item / ndt, dt = item - ib * ndt;
+  const int rb = ib < nrb ? nrb - 1 - ib : 0;
+  const int j = dt * 32 + lane;
+  const bool active = item < ndt * nrb && j < kg.M;
+  float3 dh = make_float3(0.f, 0.f, 0.f), dl = dh;
+  float inv_norm = 0.f, dnorm = 0.f;
+  if (active) {
+    const float4 h = kg.dir_hi[j], l = kg.dir_lo[j];
+    dh = make_float3(h.x, h.y, h.z);
+    dl = make_float3(l.x, l.y, l.z);
+    inv_norm = h.w;
+    dnorm = l.w;
+  }
   __shared__ float4 tile[7 * JAC_TILE];
   __shared__ float2 ctab[256];
-  stage_cis_tab(kg, ctab);
-  kcf A, NF[3], W[3];
+  __shared__ float4 krad[JAC_WARPS][R];  // (|k| hi, lo, |k| 256 / 2 pi hi, lo)
+  __shared__ float run[2 * JAC_NSUM * R * JAC_THREADS];  // running sums, then compensations
+  for (int t = threadIdx.x; t < 256; t += JAC_THREADS) ctab[t] = kg.cis_tab[t];
+  if (lane < R) {
+    const int r = rb * R + lane;
+    const bool ok = item < ndt * nrb && r < kg.L;
+    const float2 km = ok ? kg.kmag[r] : make_float2(0.f, 0.f);
+    const float2 kt = ok ? kg.kt256[r] : make_float2(0.f, 0.f);
+    krad[warp][lane] = make_float4(km.x, km.y, kt.x, kt.y);
+  }
+  for (int v = 0; v < 2 * JAC_NSUM * R; ++v) run[v * JAC_THREADS + threadIdx.x] = 0.f;
+  float acc[R][JAC_NSUM];
+#pragma unroll
+  for (int i = 0; i < R; ++i)
+#pragma unroll
+    for (int v = 0; v < JAC_NSUM; ++v) acc[i][v] = 0.f;
+  // adds the chunk's partials to the compensated running sums
+  auto flush = [&]() {
+#pragma unroll
+    for (int i = 0; i < R; ++i)
+#pragma unroll
+      for (int v = 0; v < JAC_NSUM; ++v) {
+        float* ps = run + (i * JAC_NSUM + v) * JAC_THREADS + threadIdx.x;
+        float* pc = ps + JAC_NSUM * R * JAC_THREADS;
+        const float sum = *ps, y = acc[i][v] - *pc, t = sum + y;
+        *pc = (t - sum) - y;
+        *ps = t;
+        acc[i][v] = 0.f;
+      }
+  };
   const float4* pool = b.tri_pool + 3 * od.elem_off;
   const float4* pool_lo = b.tri_lo + od.elem_off;
   const TriSrcJ* src = reinterpret_cast<const TriSrcJ*>(jo.src);
@@ -195,84 +257,129 @@ jac_affine_tri_kernel(KGridDev kg, BatchDev b, const JacObj* __restrict__ jobs, 
       tile[6 * e + 3] = make_float4((float)s.a[0], (float)s.a[1], (float)s.a[2], (float)n0x);
       tile[6 * e + 4] = make_float4((float)s.e1[0], (float)s.e1[1], (float)s.e1[2], (float)n0y);
       tile[6 * e + 5] = make_float4((float)s.e2[0], (float)s.e2[1], (float)s.e2[2], (float)n0z);
-      tile[6 * JAC_TILE + e] = pool_lo[base + e];  // centroid low word
+      tile[6 * JAC_TILE + e] = pool_lo[base + e];  // centroid low word, longest edge
     }
     __syncthreads();
-    if (!t.active) continue;
+    if (!active) continue;
     for (int e = 0; e < cnt; ++e) {
       const float4 q0 = tile[6 * e], q1 = tile[6 * e + 1], q2 = tile[6 * e + 2], ql = tile[6 * JAC_TILE + e];
-      const float3 a0 = make_float3(tile[6 * e + 3].x, tile[6 * e + 3].y, tile[6 * e + 3].z),
-                   E1 = make_float3(tile[6 * e + 4].x, tile[6 * e + 4].y, tile[6 * e + 4].z),
-                   E2 = make_float3(tile[6 * e + 5].x, tile[6 * e + 5].y, tile[6 * e + 5].z);
-      const TriNode o = tri_node(t, ctab, make_float3(q0.x, q0.y, q0.z), ql, make_float3(q1.x, q1.y, q1.z),
-                                 make_float3(q2.x, q2.y, q2.z), make_float3(q0.w, q1.w, q2.w));
-      A.fma_add(o.d.F, -2.0f * o.gam);
-      // sum_s grad_s(gamma) x0_s^T = (khat / 2) x (A [N0]_x) with [N0]_x v = v x N0
-      // (the sum over s of the gamma gradients is zero, so the vertex
-      // positions drop out): only F N0 is accumulated; khat x and A are
-      // applied once per node below
-      NF[0].fma_add(o.d.F, tile[6 * e + 3].w);
-      NF[1].fma_add(o.d.F, tile[6 * e + 4].w);
-      NF[2].fma_add(o.d.F, tile[6 * e + 5].w);
-      // W_c += gamma sum_s D_s x0_s[c] with x0 = (a0, a0 + E1, a0 + E2) and
-      // D_a + D_b + D_c = i F: gamma (i F a0[c] + D_b E1[c] + D_c E2[c])
-      const cf gF = cscale(o.d.F, o.gam), gB = cscale(o.d.Db, o.gam), gC = cscale(o.d.Dc, o.gam);
+      const float3 m = make_float3(q0.x, q0.y, q0.z), e1 = make_float3(q1.x, q1.y, q1.z),
+                   e2 = make_float3(q2.x, q2.y, q2.z);
+      const df sm = cdot2(dh, dl, m, make_float3(ql.x, ql.y, ql.z)), d1 = cdot(dh, dl, e1), d2 = cdot(dh, dl, e2);
+      const float sp = fmaxf(fmaxf(fabsf(d1.hi), fabsf(d2.hi)), fabsf(d2.hi - d1.hi));
+      const float kthr = __fdividef(2.0f, sp);           // the series for k sp < 2 (inf when sp = 0)
+      const float kshort = rcp_fast(ql.w * dnorm);       // cut after h_8 for k |e|max < 1
+      const float gam = (dh.x * q0.w + dh.y * q1.w + dh.z * q2.w) * inv_norm;
+      const TriDerPoly cp = tri_der_coeffs(d1.hi, d2.hi);
 #pragma unroll
-      for (int c = 0; c < 3; ++c) {
-        const float x = comp(a0, c), y = comp(E1, c), z = comp(E2, c);
-        W[c].add(fmaf(-gF.im, x, fmaf(gB.re, y, gC.re * z)), fmaf(gF.re, x, fmaf(gB.im, y, gC.im * z)));
-      }
-      if ((e & 15) == 15) {
-        A.flush();
+      for (int i = 0; i < R; ++i) {
+        const float4 kr = krad[warp][i];
+        const float k = kr.x;
+        cf F, Db, Dc;
+        if (k < kthr) {
+          const cf P = cis_tab_df(ctab, make_float2(kr.z, kr.w), sm);
+          const float u = k * k;
+          float fre, fim, bre, bim, cre, cim;
+          if (k < kshort) {
+            fre = poly_first<5>(cp.fa, u); fim = poly_first<3>(cp.fb, u);
+            bim = poly_first<5>(cp.ba, u); bre = poly_first<4>(cp.bb, u);
+            cim = poly_first<5>(cp.ca, u); cre = poly_first<4>(cp.cb, u);
+          } else {
+            fre = poly_u(cp.fa, u); fim = poly_u(cp.fb, u);
+            bim = poly_u(cp.ba, u); bre = poly_u(cp.bb, u);
+            cim = poly_u(cp.ca, u); cre = poly_u(cp.cb, u);
+          }
+          F = cmul(P, cf{fre, u * k * fim});
+          Db = cmul(P, cf{k * bre, bim});
+          Dc = cmul(P, cf{k * cre, cim});
+        } else {
+          const df sa = df_add(sm, df_div3(df_add(d1, d2)) * -1.0f);
+          const TriDer d = tri_generic_der_at(ctab, make_float2(kr.z, kr.w), sa, df_add(sa, d1), df_add(sa, d2),
+                                              k * d1.hi, k * d2.hi);
+          F = d.F;
+          Db = d.Db;
+          Dc = d.Dc;
+        }
+        const float4 ta = tile[6 * e + 3], tb = tile[6 * e + 4], tc = tile[6 * e + 5];
+        const float g2 = -2.0f * gam;
+        acc[i][0] = fmaf(F.re, g2, acc[i][0]);
+        acc[i][1] = fmaf(F.im, g2, acc[i][1]);
+        acc[i][2] = fmaf(F.re, ta.w, acc[i][2]);
+        acc[i][3] = fmaf(F.im, ta.w, acc[i][3]);
+        acc[i][4] = fmaf(F.re, tb.w, acc[i][4]);
+        acc[i][5] = fmaf(F.im, tb.w, acc[i][5]);
+        acc[i][6] = fmaf(F.re, tc.w, acc[i][6]);
+        acc[i][7] = fmaf(F.im, tc.w, acc[i][7]);
+        const cf gF = cscale(F, gam), gB = cscale(Db, gam), gC = cscale(Dc, gam);
+        const float a0[3] = {ta.x, ta.y, ta.z}, E1[3] = {tb.x, tb.y, tb.z}, E2[3] = {tc.x, tc.y, tc.z};
 #pragma unroll
-        for (int a = 0; a < 3; ++a) { NF[a].flush(); W[a].flush(); }
+        for (int c = 0; c < 3; ++c) {
+          acc[i][8 + 2 * c] = fmaf(-gF.im, a0[c], fmaf(gB.re, E1[c], fmaf(gC.re, E2[c], acc[i][8 + 2 * c])));
+          acc[i][9 + 2 * c] = fmaf(gF.re, a0[c], fmaf(gB.im, E1[c], fmaf(gC.im, E2[c], acc[i][9 + 2 * c])));
+        }
       }
+      if ((e & 15) == 15) flush();
     }
-    A.flush();
-#pragma unroll
-    for (int a = 0; a < 3; ++a) { NF[a].flush(); W[a].flush(); }
+    flush();
   }
-  if (!t.active) return;
-  const int64_t q = (int64_t)t.r * kg.M + t.j;
-  const cf sc = jac_out_scale(t, kg, od, q);
-  const float k = t.k.hi;
-  const cf a = cmul(A.value(), sc);
-  float2* out = G + jo.row0 * kg.Q + q;
-#pragma unroll
-  for (int r = 0; r < 3; ++r) {  // dA/dt_r = i k d_r A
-    const float kr = k * comp(t.dh, r);
-    out[(int64_t)r * kg.Q] = make_float2(-kr * a.im, kr * a.re);
-  }
+  if (!active) return;
   // MF[r][c] = sum_e F_e sum_s grad_s(gamma)_r x0_s[c] = ((khat / 2) x (A (e_c x N~)))_r, N~ = sum_e F_e N0_e
   const double* Am = jo.dofs + 3;  // A row-major
-  const cf Nt[3] = {NF[0].value(), NF[1].value(), NF[2].value()};
-  const float3 kh = make_float3(0.5f * t.dh.x * t.inv_norm, 0.5f * t.dh.y * t.inv_norm, 0.5f * t.dh.z * t.inv_norm);
-  cf MF[9];
+  float Af[9];
 #pragma unroll
-  for (int c = 0; c < 3; ++c) {
-    cf v[3];  // e_c x N~
-    v[c] = cf{0.f, 0.f};
-    v[(c + 1) % 3] = cf{-Nt[(c + 2) % 3].re, -Nt[(c + 2) % 3].im};
-    v[(c + 2) % 3] = Nt[(c + 1) % 3];
-    cf m[3];  // A v
+  for (int a = 0; a < 9; ++a) Af[a] = (float)Am[a];
+  const float3 kh = make_float3(0.5f * dh.x * inv_norm, 0.5f * dh.y * inv_norm, 0.5f * dh.z * inv_norm);
+  const double so_d = ((double)dh.x + dl.x) * od.origin[0] + ((double)dh.y + dl.y) * od.origin[1] +
+                      ((double)dh.z + dl.z) * od.origin[2];
 #pragma unroll
-    for (int i = 0; i < 3; ++i) {
-      const float a0 = (float)Am[3 * i], a1 = (float)Am[3 * i + 1], a2 = (float)Am[3 * i + 2];
-      m[i] = cf{fmaf(a0, v[0].re, fmaf(a1, v[1].re, a2 * v[2].re)), fmaf(a0, v[0].im, fmaf(a1, v[1].im, a2 * v[2].im))};
+  for (int i = 0; i < R; ++i) {
+    const int r = rb * R + i;
+    if (r >= kg.L) continue;
+    const float4 kr = krad[warp][i];
+    const float k = kr.x;
+    const int64_t q = (int64_t)r * kg.M + j;
+    // e^{ik.o} sqrt|w| (0 at k = 0, where A = 0 by definition)
+    const cf eo = cis_f64(((double)kr.x + (double)kr.y) * so_d);
+    const float sw = (k * dnorm < 1e-10f) ? 0.f : kg.sqrtw[q];
+    const cf sc = cf{eo.re * sw, eo.im * sw};
+    float sv[JAC_NSUM];
+#pragma unroll
+    for (int v = 0; v < JAC_NSUM; ++v) sv[v] = run[(i * JAC_NSUM + v) * JAC_THREADS + threadIdx.x];
+    const cf a = cmul(cf{sv[0], sv[1]}, sc);
+    float2* out = G + jo.row0 * kg.Q + q;
+#pragma unroll
+    for (int rr = 0; rr < 3; ++rr) {  // dA/dt_r = i k d_r A
+      const float kd = k * comp(dh, rr);
+      out[(int64_t)rr * kg.Q] = make_float2(-kd * a.im, kd * a.re);
     }
-    MF[c] = cf{comp(kh, 1) * m[2].re - comp(kh, 2) * m[1].re, comp(kh, 1) * m[2].im - comp(kh, 2) * m[1].im};
-    MF[3 + c] = cf{comp(kh, 2) * m[0].re - comp(kh, 0) * m[2].re, comp(kh, 2) * m[0].im - comp(kh, 0) * m[2].im};
-    MF[6 + c] = cf{comp(kh, 0) * m[1].re - comp(kh, 1) * m[0].re, comp(kh, 0) * m[1].im - comp(kh, 1) * m[0].im};
-  }
-#pragma unroll
-  for (int r = 0; r < 3; ++r)
+    const cf Nt[3] = {cf{sv[2], sv[3]}, cf{sv[4], sv[5]}, cf{sv[6], sv[7]}};
+    cf MF[9];
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
-      const cf mf = MF[3 * r + c], w = W[c].value();
-      const float kd = k * comp(t.dh, r);
-      const cf v = cmul(cf{-2.0f * (mf.re + kd * w.re), -2.0f * (mf.im + kd * w.im)}, sc);
-      out[(int64_t)(3 + 3 * r + c) * kg.Q] = make_float2(v.re, v.im);
+      cf v[3];  // e_c x N~
+      v[c] = cf{0.f, 0.f};
+      v[(c + 1) % 3] = cf{-Nt[(c + 2) % 3].re, -Nt[(c + 2) % 3].im};
+      v[(c + 2) % 3] = Nt[(c + 1) % 3];
+      cf mv[3];  // A v
+#pragma unroll
+      for (int a3 = 0; a3 < 3; ++a3) {
+        const float x0 = Af[3 * a3], x1 = Af[3 * a3 + 1], x2 = Af[3 * a3 + 2];
+        mv[a3] = cf{fmaf(x0, v[0].re, fmaf(x1, v[1].re, x2 * v[2].re)), fmaf(x0, v[0].im, fmaf(x1, v[1].im, x2 * v[2].im))};
+      }
+      MF[c] = cf{kh.y * mv[2].re - kh.z * mv[1].re, kh.y * mv[2].im - kh.z * mv[1].im};
+      MF[3 + c] = cf{kh.z * mv[0].re - kh.x * mv[2].re, kh.z * mv[0].im - kh.x * mv[2].im};
+      MF[6 + c] = cf{kh.x * mv[1].re - kh.y * mv[0].re, kh.x * mv[1].im - kh.y * mv[0].im};
     }
+#pragma unroll
+    for (int rr = 0; rr < 3; ++rr)
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        const cf mf = MF[3 * rr + c], w = cf{sv[8 + 2 * c], sv[9 + 2 * c]};
+        const float kd = k * comp(dh, rr);
+        const cf v = cmul(cf{-2.0f * (mf.re + kd * w.re), -2.0f * (mf.im + kd * w.im)}, sc);
+        out[(int64_t)(3 + 3 * rr + c) * kg.Q] = make_float2(v.re, v.im);
+      }
+  }
 }
 
 // ---- AffineDoF disks / Gaussians --------------------------------------------------------
@@ -459,7 +566,9 @@ int launch_jacobian(const pi_kgrid_impl* kg, const pi_batch_impl* b, float2* G, 
   const BatchDev B = b->dev();
   const unsigned gx = (unsigned)(((int64_t)((K.M + 31) / 32) * K.L + JAC_WARPS - 1) / JAC_WARPS);
   if (!tri.empty()) {
-    jac_affine_tri_kernel<<<dim3(gx, (unsigned)tri.size()), JAC_THREADS, 0, s>>>(K, B, d, G);
+    const int64_t items = (int64_t)((K.L + JAC_R - 1) / JAC_R) * ((K.M + 31) / 32);
+    const unsigned gxt = (unsigned)((items + JAC_WARPS - 1) / JAC_WARPS);
+    jac_affine_tri_kernel<JAC_R><<<dim3(gxt, (unsigned)tri.size()), JAC_THREADS, 0, s>>>(K, B, d, G);
     PI_LAUNCHED("jac_affine_tri_kernel");
   }
   if (!surf.empty()) {

@@ -93,6 +93,17 @@ __device__ __forceinline__ float poly_u(const float (&c)[N], float u) {
   return r;
 }
 
+// The same for the first N of the M coefficients (the series cut after h_8
+// where k |e|max < 1: 5, 3, 5, 4, 5, 4 terms of fa, fb, ba, bb, ca, cb).
+template <int N, int M>
+__device__ __forceinline__ float poly_first(const float (&c)[M], float u) {
+  static_assert(N >= 1 && N <= M, "poly_first: N out of range");
+  float r = c[N - 1];
+#pragma unroll
+  for (int i = N - 2; i >= 0; --i) r = fmaf(r, u, c[i]);
+  return r;
+}
+
 __device__ __forceinline__ TriDerPoly tri_der_coeffs(float s1, float s2) {
   const float da = -(s1 + s2) * (1.0f / 3.0f);
   const float db = s1 + da, dc = s2 + da;

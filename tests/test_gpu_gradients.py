@@ -2,9 +2,11 @@
 
 Reference pins (cpp/test/test_volume_unified.cpp:390-396, 890-896): CPU and GPU
 gradients agree to 1e-6 in FP64 and match 5-point FD to 0.01 max-abs.  The FP32
-adjoint here is held to 2e-5 of the gradient's max-abs entry against the
-oracle, and the autograd path to central FD with h = 1e-3 at 1e-2 (FD of an
-FP32 loss resolves ~1e-3 of the slope at that step).
+adjoint here is held to 1e-5 of the gradient's max-abs entry against the
+oracle (the FP32 tolerance; the worst case measured is 5.0e-6, a normal
+gradient on the 64-radius grid), and the autograd path to central FD with
+h = 1e-3 at 1e-2 (FD of an FP32 loss resolves ~1e-3 of the slope at that
+step).
 """
 import numpy as np
 import pytest
@@ -16,7 +18,7 @@ from pointint_gb300.kgrid import standard_kgrid
 
 pytestmark = pytest.mark.gpu
 
-GRAD_TOL = 2e-5
+GRAD_TOL = 1e-5
 
 
 def tangent_part(u, n):

@@ -97,6 +97,20 @@ def test_form_factors_match_oracle(cuda, orc, kg29, kind):
     check_J(Jg, Jo)
 
 
+@pytest.mark.parametrize("L", [2, 3, 6, 33])
+def test_partial_radial_blocks_match_oracle(cuda, orc, L):
+    """Radius counts that leave the last radial block partly empty: the
+    form-factor kernel takes 2 radii per thread below 4 radii, 4 below 32,
+    8 from 32 on, in pairs for its packed FP32 loops (L = 3: blocks of 2 + 1;
+    L = 6: 4 + 2; L = 33: four blocks of 8 + 1)."""
+    kg = standard_kgrid(9, L)
+    rng = np.random.default_rng(L)
+    objs = [shapes(k, rng) for k in ("ico3", "ico2_affine", "disks_affine", "gauss")]
+    Jg = gpu_J(kg, objs)
+    Jo = orc.form_factor_matrix(to_oracle(orc, objs), kg.dirs, kg.kmag)
+    check_J(Jg, Jo)
+
+
 def test_volume_matrix_matches_oracle(cuda, orc, kg29):
     rng = np.random.default_rng(42)
     objs = [shapes(k, rng) for k in KINDS]

@@ -39,8 +39,7 @@ def cis_tab_frac(idx, f):
 
 
 def cis_tab_df(kt, sm):
-    y = f32(kt[0] * sm[0])
-    t = f32(y + SHIFT)
+    t = fma(kt[0], sm[0], SHIFT)  # the exact product rounded to an integer by the shift
     n = f32(t - SHIFT)
     fr = fma(kt[0], sm[0], -n)
     fr = fma(kt[0], sm[1], fr)
