@@ -792,7 +792,7 @@ def e2e_host(kg, objs, precision, steps, evals_step, world):
             "ms_per_step": dt * 1e3, "entry_point": "pi_volume_matrix_host"}
 
 
-def profile_case(name: str):
+def profile_case(name: str, n_objects: int = 256):
     """One kernel family's workload, three times (the first launch warms up),
     with CUDA-event times printed as one JSON line.  For ncu captures of the
     kernels that the benchmark line does not time on their own:
@@ -818,7 +818,7 @@ def profile_case(name: str):
         return ts
 
     if name in ("contract", "adjoint", "jacobian", "serve"):
-        kg, objs, meta = configs.matrix256()
+        kg, objs, meta = configs.matrix256(n_objects=n_objects)
         batch = core.ObjectBatch(objs)
         J = core.form_factors(kg, batch, True)
         n = len(objs)
@@ -872,7 +872,7 @@ def main():
         print(json.dumps(line))
         return
     if args.profile_case:
-        profile_case(args.profile_case)
+        profile_case(args.profile_case, args.objects)
         return
     if args.impl == "reference":
         run_reference(args)

@@ -17,10 +17,11 @@ namespace pi {
 //   F   = e^{i pm} sum_m i^{m+2} h_m / (m+2)!,
 //   D_v = e^{i pm} sum_m i^{m+3} h_m^(v) / (m+3)!,  h_m^(v) = h_m + d_v h_{m-1}^(v),
 // truncated after m = 12.
-// Large spread: with (P, Q, R) as in tri_generic and G(h) = (e^{ih}-1-ih)/h^2,
+// Large spread: with (P, Q) the pair with the largest gap, R the middle
+// vertex, and G(h) = (e^{ih}-1-ih)/h^2,
 //   f[u,u,v] = e^{iu} G(v-u),
-//   D_R = (f[R,R,Q] - f[P,R,R]) / (Q-P),  D_Q = (f[R,Q,Q] - F) / (Q-P),
-//   D_P = (F - f[P,P,R]) / (Q-P).
+//   D_Q = (f[R,Q,Q] - F) / (Q-P),  D_P = (F - f[P,P,R]) / (Q-P),
+//   D_R = i F - D_P - D_Q.
 struct TriDer { cf F, Da, Db, Dc; };
 
 __device__ __forceinline__ cf imul(cf a) { return {-a.im, a.re}; }  // i a
@@ -160,8 +161,8 @@ __device__ __forceinline__ cf conjmul(cf a, cf b) { return {a.re * b.re + a.im *
 
 __device__ __forceinline__ cf csel(bool c, cf a, cf b) { return {c ? a.re : b.re, c ? a.im : b.im}; }
 
-// The roles (P, Q, R) are chosen by selects as in tri_generic, so lanes of a
-// warp that pick different pairs do not split.
+// The roles (P, Q the pair with the largest gap, R the middle vertex) are
+// chosen by selects, so lanes of a warp that pick different pairs do not split.
 __device__ __forceinline__ TriDer tri_generic_der(cf Pa, cf Pb, cf Pc, float al, float be) {
   TriDer d;
   d.F = tri_generic(Pa, Pb, Pc, al, be);
@@ -174,13 +175,14 @@ __device__ __forceinline__ TriDer tri_generic_der(cf Pa, cf Pb, cf Pc, float al,
   const float zP = c1 || c2 ? 0.f : al, zQ = c1 ? al : be, zR = c1 ? be : (c2 ? al : 0.f);
   const float iden = rcp_fast(zQ - zP);
   // f[u,u,v] = e^{iu} G(v - u), e^{i(v-u)} = Pv conj(Pu)
-  const cf fRRQ = cmul(phR, Gfun(conjmul(phQ, phR), zQ - zR));
-  const cf fRRP = cmul(phR, Gfun(conjmul(phP, phR), zP - zR));
   const cf fQQR = cmul(phQ, Gfun(conjmul(phR, phQ), zR - zQ));
   const cf fPPR = cmul(phP, Gfun(conjmul(phR, phP), zR - zP));
-  const cf DR = cscale(csub(fRRQ, fRRP), iden);
   const cf DQ = cscale(csub(fQQR, d.F), iden);
   const cf DP = cscale(csub(d.F, fPPR), iden);
+  // D_R from D_P + D_Q + D_R = i F (translation invariance) instead of its
+  // own two G terms: |F| <= 1/2 and |D| <= 1/6, so the subtraction costs
+  // ~1e-7 absolute, the level of the other terms' rounding
+  const cf DR = {-d.F.im - DP.re - DQ.re, d.F.re - DP.im - DQ.im};
   d.Da = csel(c1 || c2, DP, DR);
   d.Db = csel(c1, DQ, csel(c2, DR, DP));
   d.Dc = csel(c1, DR, DQ);
