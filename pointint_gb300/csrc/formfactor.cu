@@ -10,13 +10,15 @@
 //    centroid of the transformed anchors), centroids (centres) as FP32 hi + lo;
 //    the origin phase e^{ik.o} is formed and reduced in FP64 per output.
 //  * ff_kernel: one CTA = one object x 4 warps; a warp owns 32 directions
-//    (one per lane) x R radial nodes of the factored k-grid, so each element's
-//    direction dot products and series coefficients are formed once and
-//    reused for R radii.  Elements are staged through shared memory and read
-//    as broadcasts; each thread accumulates its own outputs (no reduction
-//    across threads), 16-element partials in registers and compensated
-//    running sums in shared memory; each output element is written once,
-//    coalesced, in the contraction's operand layout.
+//    (one per lane) x R neighbouring radial nodes of the factored k-grid, so
+//    each element's direction dot products and series coefficients are
+//    formed once and reused for R radii; where all R radii take the short
+//    series, two radii share each packed FP32 instruction.  Radial blocks
+//    start largest-k first, for all objects.  Elements are staged through
+//    shared memory and read as broadcasts; each thread accumulates its own
+//    outputs (no reduction across threads), 16-element partials in registers
+//    and compensated running sums in shared memory; each output element is
+//    written once, coalesced, in the contraction's operand layout.
 #include <cuda_runtime.h>
 #include <cstdint>
 #include <algorithm>
