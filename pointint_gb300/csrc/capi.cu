@@ -270,21 +270,35 @@ int pi_batch_create(const pi_object* objs, int n, int on_device, pi_stream strea
   std::stable_sort(b->order.begin(), b->order.end(),
                    [&](int a, int c) { return b->info[a].n_elems > b->info[c].n_elems; });
   auto cleanup = [&]() {
-    cudaFree(b->d_src); cudaFree(b->d_dofs); cudaFree(b->d_tri_pool); cudaFree(b->d_surf_pool);
-    cudaFree(b->d_tri_lo); cudaFree(b->d_surf_lo); cudaFree(b->d_surf_nref);
-    cudaFree(b->d_objs); cudaFree(b->d_order); cudaFree(b->d_vrow); cudaFree(b->d_vent); cudaFree(b->d_vmap);
+    cudaFree(b->d_block); cudaFree(b->d_vrow); cudaFree(b->d_vent); cudaFree(b->d_vmap);
   };
-  cudaError_t e = cudaSuccess;
-  if (e == cudaSuccess) e = cudaMalloc(&b->d_src, std::max<size_t>(src_bytes, 16));
-  if (e == cudaSuccess) e = cudaMalloc((void**)&b->d_dofs, std::max<size_t>(dof_count * sizeof(double), 16));
-  if (e == cudaSuccess) e = cudaMalloc((void**)&b->d_tri_pool, std::max<size_t>(b->n_tri * 3 * sizeof(float4), 16));
-  if (e == cudaSuccess) e = cudaMalloc((void**)&b->d_surf_pool, std::max<size_t>(b->n_surf * 2 * sizeof(float4), 16));
-  if (e == cudaSuccess) e = cudaMalloc((void**)&b->d_tri_lo, std::max<size_t>(b->n_tri * sizeof(float4), 16));
-  if (e == cudaSuccess) e = cudaMalloc((void**)&b->d_surf_lo, std::max<size_t>(b->n_surf * sizeof(float4), 16));
-  if (e == cudaSuccess) e = cudaMalloc((void**)&b->d_surf_nref, std::max<size_t>(b->n_surf * sizeof(float4), 16));
-  if (e == cudaSuccess) e = cudaMalloc((void**)&b->d_objs, std::max<size_t>(n * sizeof(ObjDev), 16));
-  if (e == cudaSuccess) e = cudaMalloc((void**)&b->d_order, std::max<size_t>(n * sizeof(int32_t), 16));
+  // one device allocation carved into the batch's buffers (256-byte aligned)
+  const size_t sizes[9] = {std::max<size_t>(src_bytes, 16),
+                           std::max<size_t>(dof_count * sizeof(double), 16),
+                           std::max<size_t>(b->n_tri * 3 * sizeof(float4), 16),
+                           std::max<size_t>(b->n_surf * 2 * sizeof(float4), 16),
+                           std::max<size_t>(b->n_tri * sizeof(float4), 16),
+                           std::max<size_t>(b->n_surf * sizeof(float4), 16),
+                           std::max<size_t>(b->n_surf * sizeof(float4), 16),
+                           std::max<size_t>(n * sizeof(ObjDev), 16),
+                           std::max<size_t>(n * sizeof(int32_t), 16)};
+  size_t offs[9], total = 0;
+  for (int i = 0; i < 9; ++i) {
+    offs[i] = total;
+    total += (sizes[i] + 255) & ~(size_t)255;
+  }
+  cudaError_t e = cudaMalloc(&b->d_block, total);
   if (e != cudaSuccess) { cleanup(); return cuda_fail(e, "pi_batch_create allocation"); }
+  unsigned char* blk = static_cast<unsigned char*>(b->d_block);
+  b->d_src = blk + offs[0];
+  b->d_dofs = reinterpret_cast<double*>(blk + offs[1]);
+  b->d_tri_pool = reinterpret_cast<float4*>(blk + offs[2]);
+  b->d_surf_pool = reinterpret_cast<float4*>(blk + offs[3]);
+  b->d_tri_lo = reinterpret_cast<float4*>(blk + offs[4]);
+  b->d_surf_lo = reinterpret_cast<float4*>(blk + offs[5]);
+  b->d_surf_nref = reinterpret_cast<float4*>(blk + offs[6]);
+  b->d_objs = reinterpret_cast<ObjDev*>(blk + offs[7]);
+  b->d_order = reinterpret_cast<int32_t*>(blk + offs[8]);
   if (on_device) {
     for (int i = 0; i < n && e == cudaSuccess; ++i) {
       const HostObjInfo& in = b->info[i];
@@ -343,9 +357,7 @@ int pi_batch_prepare(pi_batch b, pi_stream stream) {
 
 int pi_batch_destroy(pi_batch b) {
   if (!b) return PI_OK;
-  cudaFree(b->d_src); cudaFree(b->d_dofs); cudaFree(b->d_tri_pool); cudaFree(b->d_surf_pool);
-  cudaFree(b->d_tri_lo); cudaFree(b->d_surf_lo); cudaFree(b->d_surf_nref);
-  cudaFree(b->d_objs); cudaFree(b->d_order); cudaFree(b->d_vrow); cudaFree(b->d_vent); cudaFree(b->d_vmap);
+  cudaFree(b->d_block); cudaFree(b->d_vrow); cudaFree(b->d_vent); cudaFree(b->d_vmap);
   delete b;
   return PI_OK;
 }

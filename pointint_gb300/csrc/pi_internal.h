@@ -111,7 +111,8 @@ struct pi_batch_impl {
   std::vector<HostObjInfo> info;
   std::vector<int32_t> order;
   int64_t n_tri = 0, n_surf = 0;
-  // device allocations
+  // device allocations: one block (d_block) carved into the buffers below
+  void* d_block = nullptr;
   void* d_src = nullptr;     // packed reference-layout elements of all objects
   double* d_dofs = nullptr;  // all DoF vectors
   float4* d_tri_pool = nullptr;
