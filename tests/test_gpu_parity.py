@@ -375,6 +375,14 @@ def test_matrix256_subsampled_parity_and_properties(cuda, orc):
     Jo = orc.form_factor_matrix(to_oracle(orc, objs), kg.dirs, kg.kmag, stride=stride)
     sel = np.arange(0, kg.num_nodes, stride)
     check_J(J[:, sel], Jo[sel])
+    # the 256 x 256 volumes over those 1,262 nodes (their real weights), from
+    # the GPU's form factors and from the oracle's, both contracted in FP64
+    w = kg.w[sel]
+    Vg_sub = ((J[:, sel] * w) @ J[:, sel].conj().T).real / (8 * np.pi ** 3)
+    Vo_sub = ((Jo[sel].T * w) @ Jo[sel].conj()).real / (8 * np.pi ** 3)
+    err = cond_rel_err(Vg_sub, Vo_sub)
+    print(f"\nmatrix256 volumes over every {stride}th node vs the oracle: max cond rel err {err.max():.3e}")
+    assert err.max() <= VOL_TOL
     V = core.volume_matrix(kg, b).cpu().numpy()
     assert np.array_equal(V, V.T)
     # global translation leaves every V_ij unchanged
