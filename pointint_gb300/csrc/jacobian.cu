@@ -169,8 +169,9 @@ __device__ __forceinline__ TriNode tri_node(const JacThread& t, const float2* ct
 __device__ __forceinline__ float comp(float3 v, int i) { return i == 0 ? v.x : (i == 1 ? v.y : v.z); }
 
 // ---- AffineDoF triangles -------------------------------------------------------------
-// A thread owns one direction and JAC_R neighbouring radii (the warp 32
-// directions, the CTA 4 neighbouring direction blocks of one radial block).
+// A thread owns one direction and JAC_R = 4 neighbouring radii (the warp 32
+// directions, the CTA 4 neighbouring direction blocks of one radial block;
+// three CTAs per SM: 168 registers, 74 KB of shared memory each).
 // Per element and direction the small-spread series of F, D_b and D_c are
 // formed once as polynomials in k (tri_der_coeffs), so a radius costs a table
 // phasor, the Horner chains (cut after h_8 where k |e|max < 1, a test that is
@@ -181,11 +182,11 @@ __device__ __forceinline__ float comp(float3 v, int i) { return i == 0 ? v.x : (
 //   A  += -2 gamma F                                   (translations: i k d A)
 //   NF += F N0,  N0 = E1 x E2 (reference edges)        (see MF below)
 //   W  += gamma (i F a0 + D_b E1 + D_c E2)             (sum_s D_s x0_s, D_a + D_b + D_c = i F)
-constexpr int JAC_R = 2;
+constexpr int JAC_R = 4;
 constexpr int JAC_NSUM = 14;  // floats per radius: A, NF[3], W[3] (complex)
 
 template <int R>
-__global__ void __launch_bounds__(JAC_THREADS, 4)
+__global__ void __launch_bounds__(JAC_THREADS, 3)
 jac_affine_tri_kernel(KGridDev kg, BatchDev b, const JacObj* __restrict__ jobs, float2* __restrict__ G) {
   const unsigned lin = blockIdx.y * gridDim.x + blockIdx.x;
   const int slot = (int)(lin % gridDim.y), cta = (int)(lin / gridDim.y);
