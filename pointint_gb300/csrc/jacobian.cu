@@ -169,9 +169,12 @@ __device__ __forceinline__ TriNode tri_node(const JacThread& t, const float2* ct
 __device__ __forceinline__ float comp(float3 v, int i) { return i == 0 ? v.x : (i == 1 ? v.y : v.z); }
 
 // ---- AffineDoF triangles -------------------------------------------------------------
-// A thread owns one direction and JAC_R = 4 neighbouring radii (the warp 32
-// directions, the CTA 4 neighbouring direction blocks of one radial block;
-// three CTAs per SM: 168 registers, 74 KB of shared memory each).
+// A thread owns one direction and R neighbouring radii (the warp 32
+// directions, the CTA 4 neighbouring direction blocks of one radial block).
+// R = 4 (three CTAs per SM: 168 registers, 74 KB of shared memory each)
+// where the launch has at least two waves of CTAs; fewer radii per thread
+// for small launches (one moving mesh of the alignment caller), which
+// would otherwise leave SMs idle.
 // Per element and direction the small-spread series of F, D_b and D_c are
 // formed once as polynomials in k (tri_der_coeffs), so a radius costs a table
 // phasor, the Horner chains (cut after h_8 where k |e|max < 1, a test that is
@@ -182,7 +185,6 @@ __device__ __forceinline__ float comp(float3 v, int i) { return i == 0 ? v.x : (
 //   A  += -2 gamma F                                   (translations: i k d A)
 //   NF += F N0,  N0 = E1 x E2 (reference edges)        (see MF below)
 //   W  += gamma (i F a0 + D_b E1 + D_c E2)             (sum_s D_s x0_s, D_a + D_b + D_c = i F)
-constexpr int JAC_R = 4;
 constexpr int JAC_NSUM = 14;  // floats per radius: A, NF[3], W[3] (complex)
 
 template <int R>
@@ -567,9 +569,22 @@ int launch_jacobian(const pi_kgrid_impl* kg, const pi_batch_impl* b, float2* G, 
   const BatchDev B = b->dev();
   const unsigned gx = (unsigned)(((int64_t)((K.M + 31) / 32) * K.L + JAC_WARPS - 1) / JAC_WARPS);
   if (!tri.empty()) {
-    const int64_t items = (int64_t)((K.L + JAC_R - 1) / JAC_R) * ((K.M + 31) / 32);
-    const unsigned gxt = (unsigned)((items + JAC_WARPS - 1) / JAC_WARPS);
-    jac_affine_tri_kernel<JAC_R><<<dim3(gxt, (unsigned)tri.size()), JAC_THREADS, 0, s>>>(K, B, d, G);
+    // the most radii per thread that still gives two waves of CTAs
+    static int n_sm = 0;
+    if (n_sm == 0) {
+      int dev = 0;
+      if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+        n_sm = 148;
+    }
+    auto ctas = [&](int R) {
+      return (int64_t)(((int64_t)((K.L + R - 1) / R) * ((K.M + 31) / 32) + JAC_WARPS - 1) / JAC_WARPS);
+    };
+    const int64_t wave = (int64_t)n_sm * 3;
+    const int R = ctas(4) * (int64_t)tri.size() >= 2 * wave ? 4 : ctas(2) * (int64_t)tri.size() >= 2 * wave ? 2 : 1;
+    const dim3 grid((unsigned)ctas(R), (unsigned)tri.size());
+    if (R == 4) jac_affine_tri_kernel<4><<<grid, JAC_THREADS, 0, s>>>(K, B, d, G);
+    else if (R == 2) jac_affine_tri_kernel<2><<<grid, JAC_THREADS, 0, s>>>(K, B, d, G);
+    else jac_affine_tri_kernel<1><<<grid, JAC_THREADS, 0, s>>>(K, B, d, G);
     PI_LAUNCHED("jac_affine_tri_kernel");
   }
   if (!surf.empty()) {
