@@ -580,10 +580,20 @@ int launch_form_factors(const pi_kgrid_impl* kg, const pi_batch_impl* b, int sca
   const KGridDev K = kg->dev;
   const BatchDev B = b->dev();
   int R = radii_per_thread(K.L);
-  const int nrb = (K.L + R - 1) / R;
   const int ndt = (K.M + 31) / 32;
-  const int64_t items = (int64_t)nrb * ndt;
-  dim3 grid((unsigned)((items + FF_WARPS - 1) / FF_WARPS), (unsigned)b->n_obj);
+  auto ctas = [&](int r) { return ((int64_t)((K.L + r - 1) / r) * ndt + FF_WARPS - 1) / FF_WARPS; };
+  // a launch of fewer than two CTAs per SM at 8 radii per thread, such as
+  // one moving mesh of the alignment caller (76 CTAs), takes 4, which fills
+  // twice the SMs; above that 8 radii share the per-element work better
+  // (the 8-object surfel sample, 608 CTAs: 64.1 ms at 8, 68.6 ms at 4)
+  static int n_sm = 0;
+  if (n_sm == 0) {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+      n_sm = 148;
+  }
+  if (R == 8 && ctas(8) * b->n_obj < 2 * (int64_t)n_sm) R = 4;
+  dim3 grid((unsigned)ctas(R), (unsigned)b->n_obj);
   if (grid.y > 65535) return fail(PI_ERR_UNSUPPORTED, "more than 65535 objects in one batch");
   switch (R) {
     case 8: ff_kernel<8, false><<<grid, FF_THREADS, 0, s>>>(K, B, J, scale_sqrt_w, nullptr, ra); break;
