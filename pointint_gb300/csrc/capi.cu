@@ -10,6 +10,7 @@
 #include <cstring>
 #include <memory>
 #include <numeric>
+#include <unordered_map>
 #include <vector>
 #include "pi_internal.h"
 #include "group.h"
@@ -235,24 +236,47 @@ int pi_kgrid_info(pi_kgrid kg, int64_t* Q, int64_t* n_dirs, int64_t* n_radial) {
   return PI_OK;
 }
 
-int pi_batch_create(const pi_object* objs, int n, int on_device, pi_stream stream, pi_batch* out) {
+}  // extern "C"
+
+namespace {
+
+// pi_batch_create; with share_sources, objects that name the same element
+// array (pointer, count and kind) share one copy of their reference-layout
+// source on the device (instances of one mesh under different DoFs upload
+// it once).  Only batches whose sources are never replaced share them: the
+// host entry points' temporary batches.
+int batch_create_impl(const pi_object* objs, int n, int on_device, cudaStream_t s, bool share_sources,
+                      pi_batch* out) {
   if (!out) return fail(PI_ERR_INVALID_ARGUMENT, "pi_batch_create: null output");
   *out = nullptr;
   if (n < 0 || (n > 0 && !objs)) return fail(PI_ERR_INVALID_ARGUMENT, "pi_batch_create: bad object array");
-  cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
   std::unique_ptr<pi_batch_s> b(new pi_batch_s());
   b->n_obj = n;
   b->info.resize(n);
   size_t src_bytes = 0;
   int64_t dof_count = 0;
+  std::vector<char> owns_src(n, 1);  // whether object i's source is copied (first of its array)
+  std::unordered_map<const void*, int> first_of;  // element array -> first object naming it
   for (int i = 0; i < n; ++i) {
     int rc = validate_object(objs[i], i);
     if (rc) return rc;
     HostObjInfo& in = b->info[i];
     in.geom_type = objs[i].geom_type; in.dof_type = objs[i].dof_type;
     in.n_elems = objs[i].n_elems; in.n_dofs = objs[i].n_dofs;
-    in.src_off = (int64_t)src_bytes;
-    src_bytes = align16(src_bytes + (size_t)in.n_elems * elem_bytes(in.geom_type));
+    int same = -1;
+    if (share_sources && in.n_elems > 0) {
+      auto it = first_of.find(objs[i].elems);
+      if (it == first_of.end()) first_of.emplace(objs[i].elems, i);
+      else if (objs[it->second].n_elems == in.n_elems && objs[it->second].geom_type == in.geom_type)
+        same = it->second;
+    }
+    if (same >= 0) {
+      in.src_off = b->info[same].src_off;
+      owns_src[i] = 0;
+    } else {
+      in.src_off = (int64_t)src_bytes;
+      src_bytes = align16(src_bytes + (size_t)in.n_elems * elem_bytes(in.geom_type));
+    }
     in.dof_off = dof_count;
     dof_count += in.n_dofs;
     if (in.geom_type == PI_GEOM_TRIANGLE) { in.pool_off = b->n_tri; b->n_tri += in.n_elems; }
@@ -302,7 +326,7 @@ int pi_batch_create(const pi_object* objs, int n, int on_device, pi_stream strea
   if (on_device) {
     for (int i = 0; i < n && e == cudaSuccess; ++i) {
       const HostObjInfo& in = b->info[i];
-      if (in.n_elems)
+      if (in.n_elems && owns_src[i])
         e = cudaMemcpyAsync(static_cast<unsigned char*>(b->d_src) + in.src_off, objs[i].elems,
                             in.n_elems * elem_bytes(in.geom_type), cudaMemcpyDeviceToDevice, s);
       if (e == cudaSuccess)
@@ -315,7 +339,7 @@ int pi_batch_create(const pi_object* objs, int n, int on_device, pi_stream strea
     std::vector<double> hd(std::max<int64_t>(dof_count, 1));
     for (int i = 0; i < n && e == cudaSuccess; ++i) {
       const HostObjInfo& in = b->info[i];
-      if (in.n_elems)
+      if (in.n_elems && owns_src[i])
         e = cudaMemcpyAsync(static_cast<unsigned char*>(b->d_src) + in.src_off, objs[i].elems,
                             in.n_elems * elem_bytes(in.geom_type), cudaMemcpyHostToDevice, s);
       std::memcpy(hd.data() + in.dof_off, objs[i].dofs, in.n_dofs * sizeof(double));
@@ -331,6 +355,14 @@ int pi_batch_create(const pi_object* objs, int n, int on_device, pi_stream strea
   if (rc) { cleanup(); return rc; }
   *out = b.release();
   return PI_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int pi_batch_create(const pi_object* objs, int n, int on_device, pi_stream stream, pi_batch* out) {
+  return batch_create_impl(objs, n, on_device, reinterpret_cast<cudaStream_t>(stream), false, out);
 }
 
 int pi_batch_set_dofs(pi_batch b, int index, const double* d_dofs, pi_stream stream) {
@@ -502,7 +534,7 @@ int pi_volume_matrix_host(const pi_object* objs, int n, const double* dirs, cons
   int rc = pi_kgrid_create(dirs, kmag, w, Q, &kg.k);
   if (rc) return rc;
   BatchGuard b;
-  rc = pi_batch_create(objs, n, 0, reinterpret_cast<pi_stream>(s), &b.b);
+  rc = batch_create_impl(objs, n, 0, s, true, &b.b);
   if (rc) return rc;
   size_t ws_bytes = 0;
   rc = pi_contract_workspace_size(kg.k, n, precision, &ws_bytes);
@@ -544,7 +576,7 @@ static int volume_and_grads_host(const pi_object* objs, int n, const double* dir
   int rc = pi_kgrid_create(dirs, kmag, w, Q, &kg.k);
   if (rc) return rc;
   BatchGuard b;
-  rc = pi_batch_create(objs, n, 0, reinterpret_cast<pi_stream>(s), &b.b);
+  rc = batch_create_impl(objs, n, 0, s, true, &b.b);
   if (rc) return rc;
   size_t ws_c = 0, ws_a = 0;
   if ((rc = pi_contract_workspace_size(kg.k, n, PI_CONTRACT_FP32, &ws_c)) || (rc = pi_adjoint_workspace_size(kg.k, b.b, &ws_a)))
@@ -624,7 +656,7 @@ static int stacked_gram_host(const pi_object* objs, int n, const double* dirs, c
   int rc = pi_kgrid_create(dirs, kmag, w, Q, &kg.k);
   if (rc) return rc;
   BatchGuard b;
-  rc = pi_batch_create(objs, n, 0, reinterpret_cast<pi_stream>(s), &b.b);
+  rc = batch_create_impl(objs, n, 0, s, true, &b.b);
   if (rc) return rc;
   const int64_t D = dof_gradient_size(b.b), m = n + D;
   if (m > INT32_MAX) return fail(PI_ERR_UNSUPPORTED, "too many DoFs for the Hessian");

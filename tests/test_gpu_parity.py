@@ -349,16 +349,22 @@ def test_host_entry_point_matches_device_path(cuda, kg29):
 
 
 def test_host_entry_point_large_batch_matches_device_path(cuda, kg29):
-    """The host entry on a batch of 13.8 MB of elements (24 icosphere-4 meshes
-    and 8 smaller objects of every kind), its buffers carved from one device
-    block: bit for bit the device path's result."""
+    """The host entry on a batch of 13.8 MB of elements (24 instances of one
+    icosphere-4 mesh, whose element array the host entry uploads once, 4
+    copies of a second mesh, and objects of every kind), its buffers carved
+    from one device block: bit for bit the device path's result."""
     rng = np.random.default_rng(21)
     V4, F4 = G.icosphere(4)
-    objs = [G.SceneObject(G.make_triangle_mesh(V4, F4), pg.DOF_AFFINE,
+    shared = G.make_triangle_mesh(V4, F4)
+    objs = [G.SceneObject(shared, pg.DOF_AFFINE,
                           G.affine_dofs(G.random_rotation(rng) * rng.uniform(0.6, 1.4), rng.uniform(0, 4, 3)))
             for _ in range(24)]
+    other = G.make_triangle_mesh(*G.icosphere(3))
+    objs += [G.SceneObject(other, pg.DOF_AFFINE, G.affine_dofs(np.eye(3) * (1 + 0.1 * i), [0.2 * i, 0, 0]))
+             for i in range(4)]
     objs += [shapes(k, rng) for k in KINDS[:8]]
     assert sum(o.geom.elems.nbytes for o in objs) > 8 * (1 << 20)
+    assert objs[0].geom.elems is objs[23].geom.elems
     Vh = core.volume_matrix_host(kg29, objs, "fp16x3")
     Vd = core.volume_matrix(kg29, objs, "fp16x3").cpu().numpy()
     assert np.array_equal(Vh, Vd)
