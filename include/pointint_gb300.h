@@ -242,7 +242,9 @@ int pi_contract_fp32_static(const void* d_Jw, int64_t Q, int n_objects, const fl
 /* ---- one-shot host-buffer drop-ins ------------------------------------------ */
 /* compute_intersection_volume_matrix_cuda (cpp/include/compute_intersection_volume_multi_object.hpp:51-59).
  * Host objects and k-grid; V_out: host n x n.  flags: PI_VOLUME_ONLY only in
- * this entry point (gradients go through the adjoint entry points). */
+ * this entry point (gradients go through the adjoint entry points).  Objects
+ * whose elems point at the same array (same count and kind) share one upload
+ * of it; the arrays are read during the call only. */
 int pi_volume_matrix_host(const pi_object* objs, int n_objects, const double* dirs, const double* kmag,
                           const double* w, int64_t Q, int flags, int precision, double* V_out);
 /* compute_intersection_volume_cuda (cpp/include/compute_intersection_volume.hpp:48-59), volume. */
