@@ -15,7 +15,7 @@ compared are the contractions over that sub-grid's nodes, which are real nodes
 of the configuration with their real weights.  A launch on the full grid is
 checked against the oracle at the same nodes.
 
-Tolerances (spec contract): ||dJ|| / ||J|| <= 2e-6 and max |dJ| <= 1e-5
+Tolerances (the FP32 contract): ||dJ|| / ||J|| <= 2e-6 and max |dJ| <= 1e-5
 max |J| on form factors; volumes 1e-5 conditioned,
   err_ij = |dV_ij| / max(|V_ij|, 1e-3 sqrt(V_ii V_jj)).
 Gradients: 1e-5 of the largest entry against the oracle's formula gradient,

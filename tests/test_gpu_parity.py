@@ -1,6 +1,6 @@
 """GPU parity: the CUDA path (through the C ABI) against the FP64 oracle.
 
-Tolerances (spec contract): FP32 paths 1e-5 relative on volumes, using
+Tolerances (the FP32 contract): FP32 paths 1e-5 relative on volumes, using
 the conditioned relative error for off-diagonal entries
   err_ij = |dV_ij| / max(|V_ij|, 1e-3 sqrt(V_ii V_jj))
 (nearly disjoint pairs are a cancellation of O(sqrt(V_ii V_jj)) terms).  Form
