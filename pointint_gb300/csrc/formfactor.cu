@@ -16,7 +16,7 @@
 //    series, two radii share each packed FP32 instruction.  Radial blocks
 //    start largest-k first, for all objects.  Elements are staged through
 //    shared memory and read as broadcasts; each thread accumulates its own
-//    outputs (no reduction across threads), 16-element partials in registers
+//    outputs (no reduction across threads), 32-element partials in registers
 //    and compensated running sums in shared memory; each output element is
 //    written once, coalesced, in the contraction's operand layout.
 #include <cuda_runtime.h>
@@ -179,7 +179,7 @@ __global__ void prepare_elems_kernel(const PrepObj* objs, const ObjDev* od, floa
 constexpr int FF_THREADS = 128;
 constexpr int FF_WARPS = FF_THREADS / 32;
 constexpr int FF_TILE = 256;  // elements staged per shared-memory tile (a multiple of FF_CHUNK)
-constexpr int FF_CHUNK = 16;  // elements summed in FP32 before the compensated outer sum
+constexpr int FF_CHUNK = 32;  // elements summed in FP32 before the compensated outer sum
 static_assert(FF_TILE % FF_CHUNK == 0, "element chunks must not straddle tiles");
 
 // Sums over thousands of elements: each thread adds FF_CHUNK element terms into
