@@ -218,6 +218,10 @@ def run_gb300(args):
     n_tri = meta["n_triangles"]
     Q = kg.num_nodes
     evals_step = n_tri * Q
+    # the kernel evaluates one direction of each antipodal pair and writes the
+    # other from it (A(-k) = -conj A(k)): its own evaluations, for the roofline
+    n_dirs, n_eval_dirs = kg.info()[1], len(kg.direction_pairs())
+    evals_kernel = evals_step * n_eval_dirs // n_dirs
     precision = "fp16x3" if args.precision == "auto" else args.precision
     stream = torch.cuda.current_stream()
     batch = core.ObjectBatch(objs)
@@ -315,19 +319,23 @@ def run_gb300(args):
     n_sm = torch.cuda.get_device_properties(local).multi_processor_count
     ff_avg_s = ff_ms / args.steps / 1e3
     clk_max = float(peaks.get("sm_max_mhz", 2070.0))
-    fp32_achieved = FP32_FLOPS_PER_EVAL * evals_step / ff_avg_s / 1e12
+    fp32_achieved = FP32_FLOPS_PER_EVAL * evals_kernel / ff_avg_s / 1e12
     fp32_peak = n_sm * FP32_FLOPS_PER_SM_PER_CLK * clk_max * 1e6 / 1e12
-    sfu_achieved = SFU_OPS_PER_EVAL * evals_step / ff_avg_s / 1e9
+    sfu_achieved = SFU_OPS_PER_EVAL * evals_kernel / ff_avg_s / 1e9
     sfu_peak = n_sm * SFU_PER_SM_PER_CLK * clk_max * 1e6 / 1e9
     # issue slots: 4 warp instructions per SM per clock; thread instructions per
     # evaluation from the kernel's ncu capture on 32 of the 256 objects
-    issue_achieved = FF_THREAD_INSTR_PER_EVAL / 32.0 * evals_step / ff_avg_s / 1e9
+    issue_achieved = FF_THREAD_INSTR_PER_EVAL / 32.0 * evals_kernel / ff_avg_s / 1e9
     issue_peak = n_sm * 4 * clk_max * 1e6 / 1e9
     roofline = {"kernel": "ff_kernel", "bound": "fp32-issue", "achieved": fp32_achieved, "peak": fp32_peak,
                 "unit": "TFLOP/s", "frac": fp32_achieved / fp32_peak, "traffic": FF_TRAFFIC_BYTES_PER_LAUNCH,
                 "kernel_ms": ff_avg_s * 1e3, "share_of_step": (ff_ms / total_ms) if world == 1 else None,
                 "algorithmic_unit": f"{FP32_FLOPS_PER_EVAL} FP32 flops (FMA = 2) per triangle x k evaluation, the "
-                                    f"reference algorithm's count, x {evals_step:.4e} evaluations",
+                                    f"reference algorithm's count, x {evals_kernel:.4e} evaluations the kernel "
+                                    f"performs: {n_eval_dirs} of the {n_dirs} directions, one of each antipodal pair "
+                                    f"(A(-k) = -conj A(k) gives the other); the workload's {evals_step:.4e} "
+                                    "triangle x k pairs are all produced",
+                "evaluated_directions": {"evaluated": n_eval_dirs, "of": n_dirs},
                 "peak_source": f"nominal FP32: {FP32_FLOPS_PER_SM_PER_CLK} flops/clk/SM x {n_sm} SMs x {clk_max} MHz "
                                "(MEASURED_PEAKS.json holds HBM and bf16 tensor peaks only)",
                 "binding": "FP32 issue and FMA pipe: no MUFU (SFU) instructions (sine/cosine are a phasor table "

@@ -125,6 +125,16 @@ typedef struct pi_kgrid_s* pi_kgrid;
 int pi_kgrid_create(const double* dirs, const double* kmag, const double* w, int64_t Q, pi_kgrid* out);
 int pi_kgrid_destroy(pi_kgrid kg);
 int pi_kgrid_info(pi_kgrid kg, int64_t* Q, int64_t* n_dirs, int64_t* n_radial);
+/* Host only, no counterpart in the reference.  The directions a k-grid's
+ * kernels evaluate: the form factor of a real solid obeys A(-k) = -conj A(k),
+ * so of two antipodal directions (d' = -d to 1e-10 |d|; every Lebedev rule is
+ * made of such pairs) one is evaluated and the other written from it.  Writes
+ * *n_eval pairs (j, j') as 2 int32 each into out (j' = -1 for a direction
+ * without an antipode): on a tensor grid with pairs, in groups of 32 compact
+ * clusters of directions; otherwise (j, -1) in index order.  The pairing
+ * pi_kgrid_create stores.  PI_ERR_WORKSPACE_TOO_SMALL when cap < *n_eval. */
+int pi_kgrid_direction_pairs(const double* dirs, const double* kmag, int64_t Q, int32_t* out, int64_t cap,
+                             int64_t* n_eval);
 
 /* ---- device-resident object batch ------------------------------------------- */
 /* A set of objects transformed by their DoFs into the kernels' FP32 local-frame

@@ -99,6 +99,7 @@ SIGNATURES = {
     "pi_kgrid_create": (I32, [P, P, P, I64, PP]),
     "pi_kgrid_destroy": (I32, [P]),
     "pi_kgrid_info": (I32, [P, ctypes.POINTER(I64), ctypes.POINTER(I64), ctypes.POINTER(I64)]),
+    "pi_kgrid_direction_pairs": (I32, [P, P, I64, P, I64, ctypes.POINTER(I64)]),
     "pi_batch_create": (I32, [OBJP, I32, I32, P, PP]),
     "pi_batch_set_dofs": (I32, [P, I32, P, P]),
     "pi_batch_prepare": (I32, [P, P]),

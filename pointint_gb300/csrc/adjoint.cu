@@ -20,7 +20,9 @@
 //    staged once in shared memory (with the object's origin phase and the
 //    quadrature weight folded in) and read as broadcasts, while every thread
 //    recomputes its element's form factor and derivatives at each k-node and
-//    accumulates the element's parameter gradient in registers;
+//    accumulates the element's parameter gradient in registers; of two
+//    antipodal directions only one is evaluated, the other's cotangent folded
+//    into it (stage_tile);
 //  * chain kernels turn element gradients into AffineDoF gradients (fixed
 //    order FP64 block reduction per object) or TriangleMeshDoF vertex
 //    gradients (CSR gather per vertex, no atomics): results are bitwise
@@ -98,6 +100,7 @@ struct AdjStage {
   float4 dh[ADJ_DT], dl[ADJ_DT];
   float4 va[ADJ_DT];  // v = A^T dir and qd = |v|^2 (disks/Gaussians: k' = |k| v)
   double so[ADJ_DT];  // dir . origin
+  int2 jp[ADJ_DT];    // (direction, its antipode or -1); -1, -1 past the last direction
 };
 
 // Per-CTA copies of the radii (double-float |k|, and |k| in 1/256 turns per
@@ -111,13 +114,20 @@ __device__ __forceinline__ void stage_radii(const KGridDev& kg, float2* km, floa
   for (int t = threadIdx.x; t < 256; t += blockDim.x) ctab[t] = kg.cis_tab[t];
 }
 
+// The tile holds evaluated directions e0 .. e0 + ADJ_DT - 1 (KGridDev::dpair).
+// A direction's antipode contributes Re(conj(B') dA(-k)) with
+// dA(-k) = -conj dA(k) for every real parameter, which is
+// Re(conj(-conj B') dA(k)): the staged cotangent is B - conj(B') (each with
+// its own weight and origin phase) and the antipode is never evaluated.
 __device__ __forceinline__ void stage_tile(AdjStage& st, const KGridDev& kg, const ObjDev& od, const float2* Bw_obj,
-                                           const float2* km, int j0) {
+                                           const float2* km, int e0) {
   const int tid = threadIdx.x;
   if (tid < ADJ_DT) {
-    const int j = j0 + tid;
+    const int e = e0 + tid;
     float4 h = make_float4(0.f, 0.f, 0.f, 0.f), l = h;
-    if (j < kg.M) { h = kg.dir_hi[j]; l = kg.dir_lo[j]; }
+    int2 jp = make_int2(-1, -1);
+    if (e < kg.Me) { jp = kg.dpair[e]; h = kg.dir_hi[jp.x]; l = kg.dir_lo[jp.x]; }
+    st.jp[tid] = jp;
     st.dh[tid] = h;
     st.dl[tid] = l;
     const float* Am = od.A;
@@ -131,10 +141,10 @@ __device__ __forceinline__ void stage_tile(AdjStage& st, const KGridDev& kg, con
   __syncthreads();
   for (int t = tid; t < ADJ_DT * kg.L; t += blockDim.x) {
     const int jj = t / kg.L, r = t % kg.L;
-    const int j = j0 + jj;
+    const int2 jp = st.jp[jj];
     float2 v = make_float2(0.f, 0.f);
-    if (j < kg.M) {
-      const int64_t q = (int64_t)r * kg.M + j;
+    if (jp.x >= 0) {
+      const int64_t q = (int64_t)r * kg.M + jp.x;
       const df k = df{km[r].x, km[r].y};
       if (k.hi * st.dl[jj].w >= 1e-10f) {
         const float2 b = Bw_obj[q];
@@ -142,6 +152,13 @@ __device__ __forceinline__ void stage_tile(AdjStage& st, const KGridDev& kg, con
         const cf e = cis_f64(((double)k.hi + (double)k.lo) * st.so[jj]);  // e^{ik.o}
         // B e^{-ik.o} scaled: (b.x + i b.y)(e.re - i e.im)
         v = make_float2(s * (b.x * e.re + b.y * e.im), s * (b.y * e.re - b.x * e.im));
+        if (jp.y >= 0) {  // minus conj of the antipode's B' e^{+ik.o}, scaled
+          const int64_t qm = (int64_t)r * kg.M + jp.y;
+          const float2 bm = Bw_obj[qm];
+          const float sm = kg.sqrtw[qm] * (kg.sign ? kg.sign[qm] : 1.f);
+          v.x -= sm * (bm.x * e.re - bm.y * e.im);
+          v.y += sm * (bm.y * e.re + bm.x * e.im);
+        }
       }
     }
     st.B[jj * ADJ_LMAX + r] = v;
@@ -180,11 +197,11 @@ adj_surf_kernel(KGridDev kg, BatchDev b, const AdjWork* __restrict__ work, const
   const float p0 = q0.w, p1 = q1.w;
   kf gc[3], gn[3], gm[6];
   const float2* Bw_obj = Bw + (int64_t)wk.obj * kg.Q;
-  for (int j0 = 0; j0 < kg.M; j0 += ADJ_DT) {
+  for (int j0 = 0; j0 < kg.Me; j0 += ADJ_DT) {
     __syncthreads();
     stage_tile(st, kg, od, Bw_obj, km, j0);
     if (!valid) continue;
-    const int jn = min(ADJ_DT, kg.M - j0);
+    const int jn = min(ADJ_DT, kg.Me - j0);
     for (int jj = 0; jj < jn; ++jj) {
       const float4 h = st.dh[jj], l = st.dl[jj];
       const float3 dh = make_float3(h.x, h.y, h.z), dl = make_float3(l.x, l.y, l.z);
@@ -258,11 +275,11 @@ adj_tri_kernel(KGridDev kg, BatchDev b, const AdjWork* __restrict__ work, const 
                e2 = make_float3(q2.x, q2.y, q2.z), S = make_float3(q0.w, q1.w, q2.w);
   kf g[9];
   const float2* Bw_obj = Bw + (int64_t)wk.obj * kg.Q;
-  for (int j0 = 0; j0 < kg.M; j0 += ADJ_DT) {
+  for (int j0 = 0; j0 < kg.Me; j0 += ADJ_DT) {
     __syncthreads();
     stage_tile(st, kg, od, Bw_obj, km, j0);
     if (!valid) continue;
-    const int jn = min(ADJ_DT, kg.M - j0);
+    const int jn = min(ADJ_DT, kg.Me - j0);
     for (int jj = 0; jj < jn; ++jj) {
       const float4 h = st.dh[jj], l = st.dl[jj];
       const float3 dh = make_float3(h.x, h.y, h.z), dl = make_float3(l.x, l.y, l.z);

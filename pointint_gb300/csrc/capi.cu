@@ -130,17 +130,93 @@ int build_vertex_csr(pi_batch_impl* b, const pi_object* objs, int on_device, cud
 }
 struct BatchGuard { pi_batch b = nullptr; ~BatchGuard() { if (b) pi_batch_destroy(b); } };
 
-}  // namespace
+// Order `idx` (points p[3 i..3 i + 2]) into groups of `group` consecutive
+// entries that are compact in space: recursive bisection at the widest
+// coordinate, the lower part taking half the groups (so that every group but
+// the last is full).  Ties are broken by index, so the order is deterministic.
+void bisect_groups(std::vector<int>& idx, size_t lo, size_t hi, const std::vector<double>& p, size_t group) {
+  if (hi - lo <= group) return;
+  double mn[3] = {INFINITY, INFINITY, INFINITY}, mx[3] = {-INFINITY, -INFINITY, -INFINITY};
+  for (size_t t = lo; t < hi; ++t)
+    for (int c = 0; c < 3; ++c) { mn[c] = std::min(mn[c], p[3 * idx[t] + c]); mx[c] = std::max(mx[c], p[3 * idx[t] + c]); }
+  int ax = 0;
+  for (int c = 1; c < 3; ++c) if (mx[c] - mn[c] > mx[ax] - mn[ax]) ax = c;
+  std::sort(idx.begin() + lo, idx.begin() + hi, [&](int a, int b) {
+    return p[3 * a + ax] < p[3 * b + ax] || (p[3 * a + ax] == p[3 * b + ax] && a < b);
+  });
+  const size_t ng = (hi - lo + group - 1) / group, mid = lo + (ng / 2) * group;
+  bisect_groups(idx, lo, mid, p, group);
+  bisect_groups(idx, mid, hi, p, group);
+}
 
-extern "C" {
+// The evaluated directions of a k-grid (KGridDev::dpair).  v: the M
+// direction vectors (unit directions of a tensor grid, whole k vectors
+// otherwise).  Two directions pair when d_j + d_j' vanishes to 1e-10 |d_j|
+// (Lebedev tables list exact antipodes, rounded from their angles: 7e-16).
+// Each pair is evaluated at the member in the upper half-space (z > 0, then
+// y > 0, then x > 0); unpaired directions are evaluated alone.  With pairs
+// on a tensor grid the evaluated directions are ordered in compact groups
+// of 32 (one warp's lanes), so that a warp's lanes see similar projections
+// of an element and take the same branches; without pairs the identity order
+// is kept.
+std::vector<int2> direction_pairs(const std::vector<double>& v, int64_t M, bool cluster) {
+  std::vector<int> byx(M), mate(M, -1);
+  std::iota(byx.begin(), byx.end(), 0);
+  std::sort(byx.begin(), byx.end(), [&](int a, int b) { return v[3 * a] < v[3 * b] || (v[3 * a] == v[3 * b] && a < b); });
+  std::vector<double> xs(M);
+  for (int64_t t = 0; t < M; ++t) xs[t] = v[3 * byx[t]];
+  int64_t n_pairs = 0;
+  for (int64_t j = 0; j < M; ++j) {
+    if (mate[j] >= 0) continue;
+    const double* a = &v[3 * j];
+    const double nrm = std::sqrt(a[0] * a[0] + a[1] * a[1] + a[2] * a[2]);
+    if (!(nrm > 0) || !std::isfinite(nrm)) continue;
+    const double tol = 1e-10 * nrm;
+    int best = -1;
+    double best_d = tol;
+    for (auto it = std::lower_bound(xs.begin(), xs.end(), -a[0] - tol); it != xs.end() && *it <= -a[0] + tol; ++it) {
+      const int i = byx[it - xs.begin()];
+      if (i == j || mate[i] >= 0) continue;
+      const double* b = &v[3 * i];
+      const double d = std::sqrt((a[0] + b[0]) * (a[0] + b[0]) + (a[1] + b[1]) * (a[1] + b[1]) + (a[2] + b[2]) * (a[2] + b[2]));
+      if (d <= best_d) { best = i; best_d = d; }
+    }
+    if (best >= 0) { mate[j] = best; mate[best] = (int)j; ++n_pairs; }
+  }
+  std::vector<int2> out;
+  if (n_pairs == 0) {
+    out.resize(M);
+    for (int64_t j = 0; j < M; ++j) out[j] = make_int2((int)j, -1);
+    return out;
+  }
+  auto upper = [&](int j) {
+    const double* a = &v[3 * j];
+    return a[2] > 0 || (a[2] == 0 && (a[1] > 0 || (a[1] == 0 && a[0] > 0)));
+  };
+  std::vector<int> eval;
+  eval.reserve(M - n_pairs);
+  for (int64_t j = 0; j < M; ++j) {  // exactly one member of each pair
+    const int m = mate[j];
+    const bool uj = upper((int)j), um = m >= 0 && upper(m);
+    if (m < 0 || (uj != um ? uj : j < m)) eval.push_back((int)j);
+  }
+  if (cluster) {
+    std::vector<double> u(3 * M);
+    for (int64_t j = 0; j < M; ++j) {
+      const double* a = &v[3 * j];
+      const double nrm = std::sqrt(a[0] * a[0] + a[1] * a[1] + a[2] * a[2]);
+      for (int c = 0; c < 3; ++c) u[3 * j + c] = nrm > 0 ? a[c] / nrm : 0.0;
+    }
+    bisect_groups(eval, 0, eval.size(), u, 32);
+  }
+  out.resize(eval.size());
+  for (size_t t = 0; t < eval.size(); ++t) out[t] = make_int2(eval[t], mate[eval[t]]);
+  return out;
+}
 
-int pi_kgrid_create(const double* dirs, const double* kmag, const double* w, int64_t Q, pi_kgrid* out) {
-  if (!out) return fail(PI_ERR_INVALID_ARGUMENT, "pi_kgrid_create: null output");
-  *out = nullptr;
-  if (Q <= 0 || !dirs || !kmag) return fail(PI_ERR_INVALID_ARGUMENT, "pi_kgrid_create: empty k-grid");
-  if (Q > (int64_t)1 << 31) return fail(PI_ERR_UNSUPPORTED, "pi_kgrid_create: more than 2^31 nodes");
-  std::unique_ptr<pi_kgrid_s> kg(new pi_kgrid_s());
-  // Detect the reference's tensor order q = r*M + j (kgrid.hpp:33-45).
+// Detects the reference's tensor order q = r*M + j (kgrid.hpp:33-45); *M is
+// the number of directions of a tensor grid, Q otherwise.
+bool grid_layout(const double* dirs, const double* kmag, int64_t Q, int64_t* M_out) {
   int64_t M = 1;
   while (M < Q && kmag[M] == kmag[0]) ++M;
   bool tensor = (Q % M == 0);
@@ -152,13 +228,38 @@ int pi_kgrid_create(const double* dirs, const double* kmag, const double* w, int
     }
   }
   if (tensor && M > 0x7fffffff) tensor = false;
+  *M_out = tensor ? M : Q;
+  return tensor;
+}
+
+// The stored direction vectors: unit directions of a tensor grid, whole k
+// vectors (direction times |k|) otherwise.
+std::vector<double> direction_vectors(const double* dirs, const double* kmag, int64_t M, bool tensor) {
+  std::vector<double> dv(3 * M);
+  for (int64_t j = 0; j < M; ++j)
+    for (int c = 0; c < 3; ++c) dv[3 * j + c] = tensor ? dirs[3 * j + c] : dirs[3 * j + c] * kmag[j];
+  return dv;
+}
+
+}  // namespace
+
+extern "C" {
+
+int pi_kgrid_create(const double* dirs, const double* kmag, const double* w, int64_t Q, pi_kgrid* out) {
+  if (!out) return fail(PI_ERR_INVALID_ARGUMENT, "pi_kgrid_create: null output");
+  *out = nullptr;
+  if (Q <= 0 || !dirs || !kmag) return fail(PI_ERR_INVALID_ARGUMENT, "pi_kgrid_create: empty k-grid");
+  if (Q > (int64_t)1 << 31) return fail(PI_ERR_UNSUPPORTED, "pi_kgrid_create: more than 2^31 nodes");
+  std::unique_ptr<pi_kgrid_s> kg(new pi_kgrid_s());
+  int64_t M = 0;
+  const bool tensor = grid_layout(dirs, kmag, Q, &M);
   const int64_t L = tensor ? Q / M : 1;
-  if (!tensor) M = Q;
   std::vector<float4> dh(M), dl(M);
   std::vector<float2> km(L), kt(L), k256(L), tab(256);
+  const std::vector<double> dv = direction_vectors(dirs, kmag, M, tensor);
   for (int64_t j = 0; j < M; ++j) {
     double d[3];
-    for (int c = 0; c < 3; ++c) d[c] = tensor ? dirs[3 * j + c] : dirs[3 * j + c] * kmag[j];
+    for (int c = 0; c < 3; ++c) d[c] = dv[3 * j + c];
     const double nrm = std::sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
     float h[3], l[3];
     for (int c = 0; c < 3; ++c) { h[c] = (float)d[c]; l[c] = (float)(d[c] - (double)h[c]); }
@@ -193,7 +294,21 @@ int pi_kgrid_create(const double* dirs, const double* kmag, const double* w, int
   const size_t o_dh = 0, o_dl = align16(o_dh + M * sizeof(float4)), o_km = align16(o_dl + M * sizeof(float4)),
                o_sw = align16(o_km + L * sizeof(float2)), o_sg = align16(o_sw + Q * sizeof(float)),
                o_kt = align16(o_sg + Q * sizeof(float)), o_k256 = align16(o_kt + L * sizeof(float2)),
-               o_tab = align16(o_k256 + L * sizeof(float2)), total = align16(o_tab + 256 * sizeof(float2));
+               o_tab = align16(o_k256 + L * sizeof(float2)), o_pair = align16(o_tab + 256 * sizeof(float2));
+  const std::vector<int2> pairs = direction_pairs(dv, M, tensor);
+  const int64_t Me = (int64_t)pairs.size();
+  {  // every direction is written exactly once, as evaluated or as a mirror
+    std::vector<char> seen(M, 0);
+    bool ok = true;
+    for (const int2& pr : pairs) {
+      if (pr.x < 0 || pr.x >= M || pr.y < -1 || pr.y >= M || pr.y == pr.x) { ok = false; break; }
+      ok = ok && !seen[pr.x]++;
+      if (pr.y >= 0) ok = ok && !seen[pr.y]++;
+    }
+    for (int64_t j = 0; j < M && ok; ++j) ok = seen[j] == 1;
+    if (!ok) return fail(PI_ERR_UNSUPPORTED, "pi_kgrid_create: bad direction pairing");
+  }
+  const size_t total = align16(o_pair + Me * sizeof(int2));
   std::vector<unsigned char> host(total, 0);
   std::memcpy(host.data() + o_dh, dh.data(), M * sizeof(float4));
   std::memcpy(host.data() + o_dl, dl.data(), M * sizeof(float4));
@@ -203,6 +318,7 @@ int pi_kgrid_create(const double* dirs, const double* kmag, const double* w, int
   std::memcpy(host.data() + o_kt, kt.data(), L * sizeof(float2));
   std::memcpy(host.data() + o_k256, k256.data(), L * sizeof(float2));
   std::memcpy(host.data() + o_tab, tab.data(), 256 * sizeof(float2));
+  std::memcpy(host.data() + o_pair, pairs.data(), Me * sizeof(int2));
   PI_CUDA(cudaMalloc(&kg->d_mem, total));
   cudaError_t e = cudaMemcpy(kg->d_mem, host.data(), total, cudaMemcpyHostToDevice);
   if (e != cudaSuccess) { cudaFree(kg->d_mem); return cuda_fail(e, "pi_kgrid_create upload"); }
@@ -217,8 +333,24 @@ int pi_kgrid_create(const double* dirs, const double* kmag, const double* w, int
   kg->dev.kturn = reinterpret_cast<const float2*>(base + o_kt);
   kg->dev.kt256 = reinterpret_cast<const float2*>(base + o_k256);
   kg->dev.cis_tab = reinterpret_cast<const float2*>(base + o_tab);
+  kg->dev.dpair = reinterpret_cast<const int2*>(base + o_pair);
+  kg->dev.Me = (int)Me;
+  kg->Me = (int)Me;
   *out = kg.release();
   return PI_OK;
+}
+
+int pi_kgrid_direction_pairs(const double* dirs, const double* kmag, int64_t Q, int32_t* out, int64_t cap,
+                             int64_t* n_eval) {
+  if (Q <= 0 || !dirs || !kmag || !n_eval || (cap > 0 && !out))
+    return fail(PI_ERR_INVALID_ARGUMENT, "pi_kgrid_direction_pairs: bad arguments");
+  if (Q > (int64_t)1 << 31) return fail(PI_ERR_UNSUPPORTED, "pi_kgrid_direction_pairs: more than 2^31 nodes");
+  int64_t M = 0;
+  const bool tensor = grid_layout(dirs, kmag, Q, &M);
+  const std::vector<int2> pairs = direction_pairs(direction_vectors(dirs, kmag, M, tensor), M, tensor);
+  *n_eval = (int64_t)pairs.size();
+  for (int64_t t = 0; t < std::min<int64_t>(cap, *n_eval); ++t) { out[2 * t] = pairs[t].x; out[2 * t + 1] = pairs[t].y; }
+  return cap >= *n_eval ? PI_OK : fail(PI_ERR_WORKSPACE_TOO_SMALL, "pi_kgrid_direction_pairs: output too small");
 }
 
 int pi_kgrid_destroy(pi_kgrid kg) {

@@ -13,12 +13,15 @@
 //    (one per lane) x R neighbouring radial nodes of the factored k-grid, so
 //    each element's direction dot products and series coefficients are
 //    formed once and reused for R radii; where all R radii take the short
-//    series, two radii share each packed FP32 instruction.  Radial blocks
-//    start largest-k first, for all objects.  Elements are staged through
-//    shared memory and read as broadcasts; each thread accumulates its own
-//    outputs (no reduction across threads), 32-element partials in registers
-//    and compensated running sums in shared memory; each output element is
-//    written once, coalesced, in the contraction's operand layout.
+//    series, two radii share each packed FP32 instruction.  On a centrally
+//    symmetric direction set a lane evaluates one direction of an antipodal
+//    pair and writes both (A(-k) = -conj A(k) for a real solid: half the
+//    evaluations), and a warp's 32 directions form a compact cluster.  Radial
+//    blocks start largest-k first, for all objects.  Elements are staged
+//    through shared memory and read as broadcasts; each thread accumulates
+//    its own outputs (no reduction across threads), 32-element partials in
+//    registers and compensated running sums in shared memory; each output
+//    element is written once, in the contraction's operand layout.
 #include <cuda_runtime.h>
 #include <cstdint>
 #include <algorithm>
@@ -256,7 +259,7 @@ ff_kernel(KGridDev kg, BatchDev b, float2* __restrict__ J, int scale_sqrt_w, con
   const int oi = SERVE ? evals[slot].obj : b.order[slot];
   const ObjDev od = b.objs[oi];
   const int nrb = (kg.L + R - 1) / R;
-  const int ndt = (kg.M + 31) / 32;
+  const int ndt = (kg.Me + 31) / 32;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   // Warps of a CTA take neighbouring direction blocks at the same radial
   // block: they see the same radii, so they take the large-spread branch at
@@ -266,11 +269,15 @@ ff_kernel(KGridDev kg, BatchDev b, float2* __restrict__ J, int scale_sqrt_w, con
   // first (for all objects, by the re-mapping above) and the launch ends on
   // light blocks (with neighbouring radii per warp the blocks differ
   // several-fold in cost).
+  // A lane evaluates direction j = dpair[.].x and also writes its antipode
+  // jm = dpair[.].y (A(-k) = -conj A(k)), when the grid has one.
   const int item = cta * FF_WARPS + warp;
   const int ib = item / ndt, dt = item - ib * ndt;
   const int rb = ib < nrb ? nrb - 1 - ib : 0;
-  const int j = dt * 32 + lane;
-  const bool active = item < ndt * nrb && j < kg.M;
+  const int ei = dt * 32 + lane;
+  const bool active = item < ndt * nrb && ei < kg.Me;
+  int j = 0, jm = -1;
+  if (active) { const int2 pr = kg.dpair[ei]; j = pr.x; jm = pr.y; }
 
   float3 dh = make_float3(0.f, 0.f, 0.f), dl = dh;
   float inv_norm = 0.f, dnorm = 0.f;
@@ -496,9 +503,13 @@ ff_kernel(KGridDev kg, BatchDev b, float2* __restrict__ J, int scale_sqrt_w, con
         cf v{acc.sre(i), acc.sim(i)};
         if (kw[i].x * PI_TURN256 * dnorm < 1e-10f) v = cf{0.f, 0.f};  // A(0) = 0 (affine_dof.cpp:64-65)
         const float sw = kg.sqrtw[q];
-        v.re *= sw; v.im *= sw;
-        ev.dst[(int64_t)j * kg.L + r] = make_float2(v.re, v.im);
-        m = fmaxf(m, fmaxf(fabsf(v.re), fabsf(v.im)));
+        ev.dst[(int64_t)j * kg.L + r] = make_float2(v.re * sw, v.im * sw);
+        m = fmaxf(m, fmaxf(fabsf(v.re * sw), fabsf(v.im * sw)));
+        if (jm >= 0) {  // the antipode: -conj
+          const float swm = kg.sqrtw[(int64_t)r * kg.M + jm];
+          ev.dst[(int64_t)jm * kg.L + r] = make_float2(-v.re * swm, v.im * swm);
+          m = fmaxf(m, fmaxf(fabsf(v.re * swm), fabsf(v.im * swm)));
+        }
       }
     }
     atomicMax(reinterpret_cast<unsigned*>(ev.amax), __float_as_uint(m));
@@ -519,6 +530,13 @@ ff_kernel(KGridDev kg, BatchDev b, float2* __restrict__ J, int scale_sqrt_w, con
       const double kd = ((double)kw[i].x + (double)kw[i].y) * (6.283185307179586476925 / 256.0);
       cf v = cmul(cis_f64(kd * so_d), cf{acc.sre(i), acc.sim(i)});
       if (kw[i].x * PI_TURN256 * dnorm < 1e-10f) v = cf{0.f, 0.f};  // A(0) = 0 (affine_dof.cpp:64-65)
+      if (jm >= 0) {  // the antipode: -conj (the origin phase included)
+        const int64_t qm = (int64_t)r * kg.M + jm;
+        const float s = scale_sqrt_w ? kg.sqrtw[qm] : 1.0f;
+        const float2 u = make_float2(-v.re * s, v.im * s);
+        J[Jrow + qm] = u;
+        m = fmaxf(m, fmaxf(fabsf(u.x), fabsf(u.y)));
+      }
       if (scale_sqrt_w) { const float s = kg.sqrtw[q]; v.re *= s; v.im *= s; }
       J[Jrow + q] = make_float2(v.re, v.im);
       m = fmaxf(m, fmaxf(fabsf(v.re), fabsf(v.im)));
@@ -580,7 +598,7 @@ int launch_form_factors(const pi_kgrid_impl* kg, const pi_batch_impl* b, int sca
   const KGridDev K = kg->dev;
   const BatchDev B = b->dev();
   int R = radii_per_thread(K.L);
-  const int ndt = (K.M + 31) / 32;
+  const int ndt = (K.Me + 31) / 32;
   auto ctas = [&](int r) { return ((int64_t)((K.L + r - 1) / r) * ndt + FF_WARPS - 1) / FF_WARPS; };
   // a launch of fewer than two CTAs per SM at 8 radii per thread, such as
   // one moving mesh of the alignment caller (76 CTAs), takes 4, which fills
@@ -608,7 +626,7 @@ int ff_serve_threads() { return FF_THREADS; }
 
 int ff_serve_grid_x(const pi_kgrid_impl* kg) {
   const int R = radii_per_thread(kg->dev.L);
-  const int64_t items = (int64_t)((kg->dev.L + R - 1) / R) * ((kg->dev.M + 31) / 32);
+  const int64_t items = (int64_t)((kg->dev.L + R - 1) / R) * ((kg->dev.Me + 31) / 32);
   return (int)((items + FF_WARPS - 1) / FF_WARPS);
 }
 

@@ -77,7 +77,7 @@ struct kcf {
 };
 
 struct JacThread {
-  int j, r;
+  int j, jm, r;  // direction j evaluated, its antipode jm written from it (or -1)
   bool active;
   float3 dh, dl;
   float inv_norm, dnorm;
@@ -91,8 +91,11 @@ __device__ __forceinline__ JacThread jac_thread(const KGridDev& kg) {
   const int item = blockIdx.x * JAC_WARPS + warp;
   const int dt = item / kg.L;
   t.r = item - dt * kg.L;
-  t.j = dt * 32 + lane;
-  t.active = dt < (kg.M + 31) / 32 && t.j < kg.M;
+  const int ei = dt * 32 + lane;
+  t.active = dt < (kg.Me + 31) / 32 && ei < kg.Me;
+  t.j = 0;
+  t.jm = -1;
+  if (t.active) { const int2 pr = kg.dpair[ei]; t.j = pr.x; t.jm = pr.y; }
   t.dh = t.dl = make_float3(0.f, 0.f, 0.f);
   t.inv_norm = t.dnorm = 0.f;
   t.k = df{0.f, 0.f};
@@ -117,13 +120,33 @@ __device__ __forceinline__ void stage_cis_tab(const KGridDev& kg, float2* ctab) 
   __syncthreads();
 }
 
-// e^{ik.o} sqrt|w| for this thread's node (0 at k = 0, where A = 0 by definition).
-__device__ __forceinline__ cf jac_out_scale(const JacThread& t, const KGridDev& kg, const ObjDev& od, int64_t q) {
+// e^{ik.o} for this thread's node (0 at k = 0, where A = 0 by definition).
+__device__ __forceinline__ cf jac_origin_phase(const JacThread& t, const ObjDev& od) {
   const double so_d = ((double)t.dh.x + t.dl.x) * od.origin[0] + ((double)t.dh.y + t.dl.y) * od.origin[1] +
                       ((double)t.dh.z + t.dl.z) * od.origin[2];
   const cf e = cis_f64(((double)t.k.hi + (double)t.k.lo) * so_d);
-  const float s = (t.k.hi * t.dnorm < 1e-10f) ? 0.f : kg.sqrtw[q];
-  return cf{e.re * s, e.im * s};
+  return (t.k.hi * t.dnorm < 1e-10f) ? cf{0.f, 0.f} : e;
+}
+
+// The node of radius r and direction j, and that of its antipode jm: a
+// derivative of a real solid's form factor obeys dA(-k) = -conj dA(k) like A,
+// so one evaluation gives both outputs, each scaled by its own sqrt|w|.
+struct JacOut {
+  int64_t q, qm;  // qm < 0: no antipode
+  float sw, swm;
+  __device__ __forceinline__ void put(float2* row, cf v) const {
+    row[q] = make_float2(v.re * sw, v.im * sw);
+    if (qm >= 0) row[qm] = make_float2(-v.re * swm, v.im * swm);
+  }
+};
+
+__device__ __forceinline__ JacOut jac_out(const KGridDev& kg, int r, int j, int jm) {
+  JacOut o;
+  o.q = (int64_t)r * kg.M + j;
+  o.qm = jm >= 0 ? (int64_t)r * kg.M + jm : -1;
+  o.sw = kg.sqrtw[o.q];
+  o.swm = jm >= 0 ? kg.sqrtw[o.qm] : 0.f;
+  return o;
 }
 
 // Triangle derivative pieces at one node: F, D_a, D_b, D_c (tri_adjoint.cuh),
@@ -194,13 +217,15 @@ jac_affine_tri_kernel(KGridDev kg, BatchDev b, const JacObj* __restrict__ jobs, 
   const int slot = (int)(lin % gridDim.y), cta = (int)(lin / gridDim.y);
   const JacObj jo = jobs[slot];
   const ObjDev od = b.objs[jo.obj];
-  const int nrb = (kg.L + R - 1) / R, ndt = (kg.M + 31) / 32;
+  const int nrb = (kg.L + R - 1) / R, ndt = (kg.Me + 31) / 32;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int item = cta * JAC_WARPS + warp;
   const int ib = item / ndt, dt = item - ib * ndt;
   const int rb = ib < nrb ? nrb - 1 - ib : 0;
-  const int j = dt * 32 + lane;
-  const bool active = item < ndt * nrb && j < kg.M;
+  const int ei = dt * 32 + lane;
+  const bool active = item < ndt * nrb && ei < kg.Me;
+  int j = 0, jm = -1;  // direction evaluated, its antipode written from it (or -1)
+  if (active) { const int2 pr = kg.dpair[ei]; j = pr.x; jm = pr.y; }
   float3 dh = make_float3(0.f, 0.f, 0.f), dl = dh;
   float inv_norm = 0.f, dnorm = 0.f;
   if (active) {
@@ -340,20 +365,19 @@ jac_affine_tri_kernel(KGridDev kg, BatchDev b, const JacObj* __restrict__ jobs, 
     if (r >= kg.L) continue;
     const float4 kr = krad[warp][i];
     const float k = kr.x;
-    const int64_t q = (int64_t)r * kg.M + j;
-    // e^{ik.o} sqrt|w| (0 at k = 0, where A = 0 by definition)
+    const JacOut o = jac_out(kg, r, j, jm);
+    // e^{ik.o} (0 at k = 0, where A = 0 by definition); sqrt|w| at the store
     const cf eo = cis_f64(((double)kr.x + (double)kr.y) * so_d);
-    const float sw = (k * dnorm < 1e-10f) ? 0.f : kg.sqrtw[q];
-    const cf sc = cf{eo.re * sw, eo.im * sw};
+    const cf sc = (k * dnorm < 1e-10f) ? cf{0.f, 0.f} : eo;
     float sv[JAC_NSUM];
 #pragma unroll
     for (int v = 0; v < JAC_NSUM; ++v) sv[v] = run[(i * JAC_NSUM + v) * JAC_THREADS + threadIdx.x];
     const cf a = cmul(cf{sv[0], sv[1]}, sc);
-    float2* out = G + jo.row0 * kg.Q + q;
+    float2* out = G + jo.row0 * kg.Q;
 #pragma unroll
     for (int rr = 0; rr < 3; ++rr) {  // dA/dt_r = i k d_r A
       const float kd = k * comp(dh, rr);
-      out[(int64_t)rr * kg.Q] = make_float2(-kd * a.im, kd * a.re);
+      o.put(out + (int64_t)rr * kg.Q, cf{-kd * a.im, kd * a.re});
     }
     const cf Nt[3] = {cf{sv[2], sv[3]}, cf{sv[4], sv[5]}, cf{sv[6], sv[7]}};
     cf MF[9];
@@ -380,7 +404,7 @@ jac_affine_tri_kernel(KGridDev kg, BatchDev b, const JacObj* __restrict__ jobs, 
         const cf mf = MF[3 * rr + c], w = cf{sv[8 + 2 * c], sv[9 + 2 * c]};
         const float kd = k * comp(dh, rr);
         const cf v = cmul(cf{-2.0f * (mf.re + kd * w.re), -2.0f * (mf.im + kd * w.im)}, sc);
-        out[(int64_t)(3 + 3 * rr + c) * kg.Q] = make_float2(v.re, v.im);
+        o.put(out + (int64_t)(3 + 3 * rr + c) * kg.Q, v);
       }
   }
 }
@@ -458,19 +482,19 @@ jac_affine_surf_kernel(KGridDev kg, BatchDev b, const JacObj* __restrict__ jobs,
     for (int a = 0; a < 3; ++a) { Z[a].flush(); N[a].flush(); }
   }
   if (!t.active) return;
-  const int64_t q = (int64_t)t.r * kg.M + t.j;
-  const cf scl = jac_out_scale(t, kg, od, q);
+  const JacOut o = jac_out(kg, t.r, t.j, t.jm);
+  const cf scl = jac_origin_phase(t, od);
   const double* Am = jo.dofs + 3;  // A row-major
   float atd[3];  // (A^T d)_c = sum_p d_p A_pc
 #pragma unroll
   for (int c = 0; c < 3; ++c)
     atd[c] = (float)(t.dh.x * Am[c] + t.dh.y * Am[3 + c] + t.dh.z * Am[6 + c]);
   const cf a = cmul(A.value(), scl), y = Y.value();
-  float2* out = G + jo.row0 * kg.Q + q;
+  float2* out = G + jo.row0 * kg.Q;
 #pragma unroll
   for (int r = 0; r < 3; ++r) {
     const float kr = k * comp(t.dh, r);
-    out[(int64_t)r * kg.Q] = make_float2(-kr * a.im, kr * a.re);
+    o.put(out + (int64_t)r * kg.Q, cf{-kr * a.im, kr * a.re});
   }
 #pragma unroll
   for (int r = 0; r < 3; ++r)
@@ -481,7 +505,7 @@ jac_affine_surf_kernel(KGridDev kg, BatchDev b, const JacObj* __restrict__ jobs,
       // i k d_r Z_c + khat_r N_c + k^2 d_r (A^T d)_c Y
       const float f = k2 * dr * atd[c], g = dr * t.inv_norm, kd = k * dr;
       const cf v = cmul(cf{-kd * z.im + g * nn.re + f * y.re, kd * z.re + g * nn.im + f * y.im}, scl);
-      out[(int64_t)(3 + 3 * r + c) * kg.Q] = make_float2(v.re, v.im);
+      o.put(out + (int64_t)(3 + 3 * r + c) * kg.Q, v);
     }
 }
 
@@ -495,8 +519,8 @@ jac_mesh_kernel(KGridDev kg, BatchDev b, const JacObj* __restrict__ jobs, const 
   __shared__ float2 ctab[256];
   stage_cis_tab(kg, ctab);
   if (!t.active) return;
-  const int64_t q = (int64_t)t.r * kg.M + t.j;
-  const cf scl = jac_out_scale(t, kg, od, q);
+  const JacOut o = jac_out(kg, t.r, t.j, t.jm);
+  const cf scl = jac_origin_phase(t, od);
   const float k = t.k.hi;
   for (int64_t v = jo.vstart; v < jo.vstart + jo.nverts; ++v) {
     float gr[3] = {0.f, 0.f, 0.f}, gi[3] = {0.f, 0.f, 0.f};
@@ -520,8 +544,7 @@ jac_mesh_kernel(KGridDev kg, BatchDev b, const JacObj* __restrict__ jobs, const 
     const int64_t row = vmap[v];
 #pragma unroll
     for (int r = 0; r < 3; ++r) {
-      const cf val = cmul(cf{gr[r], gi[r]}, scl);
-      G[(row + r) * kg.Q + q] = make_float2(val.re, val.im);
+      o.put(G + (row + r) * kg.Q, cmul(cf{gr[r], gi[r]}, scl));
     }
   }
 }
@@ -567,7 +590,7 @@ int launch_jacobian(const pi_kgrid_impl* kg, const pi_batch_impl* b, float2* G, 
   PI_CUDA(cudaMemcpyAsync(d, all.data(), nj * sizeof(JacObj), cudaMemcpyHostToDevice, s));
   const KGridDev K = kg->dev;
   const BatchDev B = b->dev();
-  const unsigned gx = (unsigned)(((int64_t)((K.M + 31) / 32) * K.L + JAC_WARPS - 1) / JAC_WARPS);
+  const unsigned gx = (unsigned)(((int64_t)((K.Me + 31) / 32) * K.L + JAC_WARPS - 1) / JAC_WARPS);
   if (!tri.empty()) {
     // the most radii per thread that still gives two waves of CTAs
     static int n_sm = 0;
@@ -577,7 +600,7 @@ int launch_jacobian(const pi_kgrid_impl* kg, const pi_batch_impl* b, float2* G, 
         n_sm = 148;
     }
     auto ctas = [&](int R) {
-      return (int64_t)(((int64_t)((K.L + R - 1) / R) * ((K.M + 31) / 32) + JAC_WARPS - 1) / JAC_WARPS);
+      return (int64_t)(((int64_t)((K.L + R - 1) / R) * ((K.Me + 31) / 32) + JAC_WARPS - 1) / JAC_WARPS);
     };
     const int64_t wave = (int64_t)n_sm * 3;
     const int R = ctas(4) * (int64_t)tri.size() >= 2 * wave ? 4 : ctas(2) * (int64_t)tri.size() >= 2 * wave ? 2 : 1;

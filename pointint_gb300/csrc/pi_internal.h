@@ -43,6 +43,14 @@ struct KGridDev {
   const float2* kturn;    // L: kmag / 2 pi (hi, lo)
   const float2* kt256;    // L: kmag 256 / 2 pi (hi, lo): phases in units of 1/256 turn
   const float2* cis_tab;  // 256: e^{2 pi i j / 256} (cos, sin), rounded once from FP64
+  // Evaluated directions: Me entries (j, j'), j' the direction antipodal to j
+  // (d_j' = -d_j) or -1.  The form factor of a real solid satisfies
+  // A(-k) = -conj A(k), so the kernels that produce per-node outputs evaluate
+  // direction j only and write j' from it.  On a centrally symmetric
+  // direction set (every Lebedev rule) Me = M / 2, the entries grouped 32 at
+  // a time into compact clusters of directions; otherwise (j, -1) in order.
+  const int2* dpair;
+  int Me;
 };
 
 struct pi_kgrid_impl {
@@ -51,6 +59,7 @@ struct pi_kgrid_impl {
   std::vector<double> w;        // host copy of weights
   int64_t Q = 0;
   int M = 0, L = 0;
+  int Me = 0;                   // evaluated directions (dev.dpair)
   bool tensor = false;
   bool all_positive = true;
 };

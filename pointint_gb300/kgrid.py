@@ -73,6 +73,17 @@ class KGrid:
         _lib.check(_lib.lib().pi_kgrid_info(self.handle(), ctypes.byref(Q), ctypes.byref(M), ctypes.byref(L)))
         return Q.value, M.value, L.value
 
+    def direction_pairs(self) -> np.ndarray:
+        """(n_eval, 2) int32: the directions the kernels evaluate, each with
+        its antipode (or -1), in evaluation order (host only; the pairing the
+        device k-grid stores)."""
+        Q = self.num_nodes
+        out = np.zeros((Q, 2), dtype=np.int32)
+        n = ctypes.c_int64()
+        _lib.check(_lib.lib().pi_kgrid_direction_pairs(self.dirs.ctypes.data, self.kmag.ctypes.data, Q,
+                                                       out.ctypes.data, Q, ctypes.byref(n)))
+        return out[:n.value].copy()
+
     def __del__(self):
         h = getattr(self, "_handle", None)
         if h is not None and _lib._lib is not None:
