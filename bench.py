@@ -383,22 +383,25 @@ def run_gb300(args):
 
 
 # DRAM bytes (read + write) of one full-size ff_kernel launch.  Reads: captured
-# with ncu on 32 of the 256 objects (82,112 triangles: 5.93 MB with the
-# centroid low words) and scaled by
-# the triangle count (656,896 / 82,112), since element reads grow with the
-# elements.  Writes: that capture's J (19.7 MB) stayed in L2, but the full
-# J (256 x 76,928 complex64 = 157.5 MB) exceeds the 129 MB L2 and is counted
-# as written once.
-FF_TRAFFIC_BYTES_PER_LAUNCH = 5.93e6 * 656896 / 82112 + 256 * 76928 * 8
-# Thread instructions per triangle x k evaluation of ff_kernel, from its ncu
-# capture on 32 of the 256 objects (smsp__inst_executed.sum 9.336e9 x 32 /
-# 6.317e9 evaluations; packed FP32 instructions count once).
-FF_THREAD_INSTR_PER_EVAL = 47.3
-# The same capture's FMA-pipe busy share (sm__pipe_fma_cycles_active, 62.4%
+# with ncu on 32 of the 256 objects (82,112 triangles: 5.70 MB with the
+# centroid low words) and scaled by the triangle count (656,896 / 82,112),
+# since element reads grow with the elements.  Writes: that capture's J
+# (19.7 MB) stayed in L2, but the full J (256 x 76,928 complex64 = 157.5 MB)
+# exceeds the 129 MB L2 and is counted as written once.
+FF_TRAFFIC_BYTES_PER_LAUNCH = 5.70e6 * 656896 / 82112 + 256 * 76928 * 8
+# Thread instructions per evaluation the kernel performs (one direction of
+# each antipodal pair), from its ncu capture on 32 of the 256 objects
+# (smsp__inst_executed.sum 4.481e9 x 32 / 3.158e9 evaluations; packed FP32
+# instructions count once).
+FF_THREAD_INSTR_PER_EVAL = 45.4
+# The same capture's FMA-pipe busy share (sm__pipe_fma_cycles_active, 51.0%
 # of active cycles, packed FP32 instructions holding the pipe two cycles) and
-# issue-slot share (smsp__issue_active, 73.3%).
-FF_FMA_PIPE_ACTIVE = 0.624
-FF_ISSUE_ACTIVE = 0.733
+# issue-slot share (smsp__issue_active, 59.0%).  The 32-object launch is 1.6
+# waves of CTAs and ends on a tail (2.8 warps per scheduler on average), so
+# both read lower than in the 256-object launch, whose issue share the line's
+# `issue.frac` gives from its own time.
+FF_FMA_PIPE_ACTIVE = 0.510
+FF_ISSUE_ACTIVE = 0.590
 
 
 def _pcts(ms):
