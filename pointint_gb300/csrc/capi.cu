@@ -160,11 +160,21 @@ void bisect_groups(std::vector<int>& idx, size_t lo, size_t hi, const std::vecto
 // of an element and take the same branches; without pairs the identity order
 // is kept.
 std::vector<int2> direction_pairs(const std::vector<double>& v, int64_t M, bool cluster) {
+  // candidates by the coordinate with the widest range (a planar set of k
+  // vectors would put every point at one value of the others)
+  int ax = 0;
+  {
+    double mn[3] = {INFINITY, INFINITY, INFINITY}, mx[3] = {-INFINITY, -INFINITY, -INFINITY};
+    for (int64_t j = 0; j < M; ++j)
+      for (int c = 0; c < 3; ++c) { mn[c] = std::min(mn[c], v[3 * j + c]); mx[c] = std::max(mx[c], v[3 * j + c]); }
+    for (int c = 1; c < 3; ++c) if (mx[c] - mn[c] > mx[ax] - mn[ax]) ax = c;
+  }
   std::vector<int> byx(M), mate(M, -1);
   std::iota(byx.begin(), byx.end(), 0);
-  std::sort(byx.begin(), byx.end(), [&](int a, int b) { return v[3 * a] < v[3 * b] || (v[3 * a] == v[3 * b] && a < b); });
+  std::sort(byx.begin(), byx.end(),
+            [&](int a, int b) { return v[3 * a + ax] < v[3 * b + ax] || (v[3 * a + ax] == v[3 * b + ax] && a < b); });
   std::vector<double> xs(M);
-  for (int64_t t = 0; t < M; ++t) xs[t] = v[3 * byx[t]];
+  for (int64_t t = 0; t < M; ++t) xs[t] = v[3 * byx[t] + ax];
   int64_t n_pairs = 0;
   for (int64_t j = 0; j < M; ++j) {
     if (mate[j] >= 0) continue;
@@ -174,7 +184,7 @@ std::vector<int2> direction_pairs(const std::vector<double>& v, int64_t M, bool 
     const double tol = 1e-10 * nrm;
     int best = -1;
     double best_d = tol;
-    for (auto it = std::lower_bound(xs.begin(), xs.end(), -a[0] - tol); it != xs.end() && *it <= -a[0] + tol; ++it) {
+    for (auto it = std::lower_bound(xs.begin(), xs.end(), -a[ax] - tol); it != xs.end() && *it <= -a[ax] + tol; ++it) {
       const int i = byx[it - xs.begin()];
       if (i == j || mate[i] >= 0) continue;
       const double* b = &v[3 * i];

@@ -100,3 +100,22 @@ def test_oracle_form_factor_is_antisymmetric_hermitian():
     for o in (tri, disk, gau):
         a, b = orc.form_factor(o, k), orc.form_factor(o, -k)
         assert np.abs(b + np.conj(a)).max() <= 1e-12 * np.abs(a).max()
+
+
+def test_planar_node_list_pairs_quickly():
+    # every k vector in the x = 0 plane: candidates are searched along the
+    # widest coordinate, so this stays fast and pairs every point
+    import time
+    rng = np.random.default_rng(5)
+    n = 20000
+    ang = rng.uniform(0.0, np.pi, n)
+    r = rng.uniform(0.5, 2.0, n)
+    k = np.stack([np.zeros(n), np.cos(ang) * r, np.sin(ang) * r], axis=1)
+    k = np.concatenate([k, -k])
+    kmag = np.linalg.norm(k, axis=1)
+    t0 = time.perf_counter()
+    p = kgrid.KGrid(k / kmag[:, None], kmag, np.ones(len(kmag))).direction_pairs()
+    assert time.perf_counter() - t0 < 5.0
+    assert len(p) == n and (p[:, 1] >= 0).all()
+    assert (_coverage(p, 2 * n) == 1).all()
+    assert np.abs(k[p[:, 0]] + k[p[:, 1]]).max() < 1e-12
