@@ -288,11 +288,7 @@ __global__ void reduce_tiles_kernel(const float* __restrict__ partials, const Sy
   V[(int64_t)j * g.n + i] = s;
 }
 
-int sm_count() {
-  int dev = 0, sms = 148;
-  if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  return sms;
-}
+int sm_count() { return current_sm_count(); }
 
 // K ranges: a diagonal tile's 3 quadrants get 4/3 of an off-diagonal tile's
 // k per CTA (s_d : s_o = 3 : 4), with as many CTAs as fit in one wave of one
@@ -330,12 +326,9 @@ bool vector_loads_ok(const void* X, int64_t K) {
 }
 
 int launch_syrk(const float* X, const SyrkGeom& g, const float* sign, float* partials, double* V, cudaStream_t s) {
-  static std::once_flag once;
-  static cudaError_t attr = cudaSuccess;
-  std::call_once(once, [] {
-    attr = cudaFuncSetAttribute(syrk_fp32_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SYRK_SMEM);
-  });
-  if (attr != cudaSuccess) return cuda_fail(attr, "cudaFuncSetAttribute(syrk_fp32_kernel)");
+  const int attr = ensure_smem_limit(reinterpret_cast<const void*>(syrk_fp32_kernel), (int)SYRK_SMEM,
+                                     "cudaFuncSetAttribute(syrk_fp32_kernel)");
+  if (attr != PI_OK) return attr;
   const int64_t ctas = syrk_tiles(g);
   if (ctas > 0x7fffffffLL) return fail(PI_ERR_UNSUPPORTED, "too many objects for the FP32 contraction");
   syrk_fp32_kernel<<<(unsigned)ctas, NT, SYRK_SMEM, s>>>(X, g, sign, vector_loads_ok(X, g.K), partials);

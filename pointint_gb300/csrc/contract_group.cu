@@ -549,24 +549,11 @@ __global__ void group_single_setup_kernel(GRow* rows, GQuery* query, GHeader* hd
   }
 }
 
-int g_sms = 0;
-std::once_flag g_attr_once;
 // Testing hooks (pi_test_set_contract_faults): the wait limit and the chunk
 // that CTA 0's loader skips, read when a single-matrix contraction is set up.
 std::atomic<long long> g_test_wait_cycles{0};
 std::atomic<long long> g_test_starve_chunk{-1};
-int g_attr_rc = PI_OK;
-
-int sms() {
-  if (g_sms == 0) {
-    int dev = 0, v = 0;
-    if (cudaGetDevice(&dev) == cudaSuccess && cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess && v > 0)
-      g_sms = v;
-    else
-      return 148;
-  }
-  return g_sms;
-}
+int sms() { return current_sm_count(); }
 
 struct SinglePlan {
   int nt, npairs, nsplit, nchunks, items;
@@ -617,13 +604,11 @@ const void* group_contract_fn(int op, int phase, int all_tma) { return fn_of(op,
 const void* group_reduce_fn() { return reinterpret_cast<const void*>(group_reduce_kernel); }
 
 int group_prepare_attributes() {
-  std::call_once(g_attr_once, [] {
-    for (int v = 0; v < 8; ++v) {
-      cudaError_t e = cudaFuncSetAttribute(fn_of(v & 1, (v >> 1) & 1, v >> 2), cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM);
-      if (e != cudaSuccess) { g_attr_rc = cuda_fail(e, "cudaFuncSetAttribute(group_split3_kernel)"); return; }
-    }
-  });
-  return g_attr_rc;
+  for (int v = 0; v < 8; ++v) {
+    const int rc = ensure_smem_limit(fn_of(v & 1, (v >> 1) & 1, v >> 2), (int)SMEM, "cudaFuncSetAttribute(group_split3_kernel)");
+    if (rc != PI_OK) return rc;
+  }
+  return PI_OK;
 }
 
 int launch_group_contract(const GroupDev& g, const CUtensorMap* xmap, bool all_tma, int grid, cudaStream_t s) {

@@ -286,8 +286,7 @@ TcPlan plan_tc(int64_t Q, int n, int kind) {
   p.npairs = p.nt * (p.nt + 1) / 2;
   const int64_t kc = kind == KIND_BF16 ? 64 : 32;
   p.nchunks = (p.K + kc - 1) / kc;
-  int dev = 0, sms = 148;
-  if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const int sms = current_sm_count();
   // At least one CTA per SM, and at most TC_MAX_CHUNKS chunks (48-96 MMAs
   // each) per accumulator: the tensor cores' FP32 accumulation error grows
   // with the number of MMAs summed into one accumulator.
@@ -344,13 +343,11 @@ int launch_contract_tc(const pi_kgrid_impl* kg, const float2* Jw, int n, int kin
   const size_t need = 256 + (size_t)p.nsplit * p.npairs * TC_M * TC_M * sizeof(float);
   if (ws_bytes < need || !ws) return fail(PI_ERR_WORKSPACE_TOO_SMALL, "tensor-core contraction workspace too small");
   if ((reinterpret_cast<uintptr_t>(Jw) & 15) != 0) return fail(PI_ERR_INVALID_ARGUMENT, "J must be 16-byte aligned");
-  static bool attr_set[2] = {false, false};
-  if (!attr_set[kind]) {
-    if (kind == KIND_BF16)
-      PI_CUDA(cudaFuncSetAttribute(syrk_split3_kernel<KIND_BF16>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
-    else
-      PI_CUDA(cudaFuncSetAttribute(syrk_split3_kernel<KIND_TF32>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
-    attr_set[kind] = true;
+  {
+    const void* fn = kind == KIND_BF16 ? reinterpret_cast<const void*>(syrk_split3_kernel<KIND_BF16>)
+                                       : reinterpret_cast<const void*>(syrk_split3_kernel<KIND_TF32>);
+    const int rc = ensure_smem_limit(fn, (int)SMEM_BYTES, "cudaFuncSetAttribute(syrk_split3_kernel)");
+    if (rc != PI_OK) return rc;
   }
   int* err = static_cast<int*>(ws);
   float* partials = reinterpret_cast<float*>(static_cast<unsigned char*>(ws) + 256);

@@ -604,12 +604,7 @@ int launch_form_factors(const pi_kgrid_impl* kg, const pi_batch_impl* b, int sca
   // one moving mesh of the alignment caller (76 CTAs), takes 4, which fills
   // twice the SMs; above that 8 radii share the per-element work better
   // (the 8-object surfel sample, 608 CTAs: 64.1 ms at 8, 68.6 ms at 4)
-  static int n_sm = 0;
-  if (n_sm == 0) {
-    int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
-      n_sm = 148;
-  }
+  const int n_sm = current_sm_count();
   if (R == 8 && ctas(8) * b->n_obj < 2 * (int64_t)n_sm) R = 4;
   dim3 grid((unsigned)ctas(R), (unsigned)b->n_obj);
   if (grid.y > 65535) return fail(PI_ERR_UNSUPPORTED, "more than 65535 objects in one batch");

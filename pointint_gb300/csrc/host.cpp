@@ -9,6 +9,9 @@
 #include <string>
 #include <vector>
 #include <atomic>
+#include <map>
+#include <mutex>
+#include <utility>
 #include "pi_internal.h"
 
 namespace pi {
@@ -28,6 +31,28 @@ int cuda_fail(cudaError_t e, const char* what) {
   return e == cudaErrorMemoryAllocation ? PI_ERR_OUT_OF_MEMORY : PI_ERR_CUDA;
 }
 void count_launch(int n) { g_launches += n; }
+
+int current_sm_count() {
+  int dev = 0, sms = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+      sms <= 0)
+    return 148;
+  return sms;
+}
+
+int ensure_smem_limit(const void* fn, int bytes, const char* what) {
+  static std::mutex mu;
+  static std::map<std::pair<const void*, int>, cudaError_t> done;  // (function, device) -> result
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
+  std::lock_guard<std::mutex> lock(mu);
+  auto it = done.find({fn, dev});
+  if (it == done.end())
+    it = done.emplace(std::make_pair(fn, dev), cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes))
+             .first;
+  return it->second == cudaSuccess ? PI_OK : cuda_fail(it->second, what);
+}
 
 }  // namespace pi
 

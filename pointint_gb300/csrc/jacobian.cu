@@ -593,12 +593,7 @@ int launch_jacobian(const pi_kgrid_impl* kg, const pi_batch_impl* b, float2* G, 
   const unsigned gx = (unsigned)(((int64_t)((K.Me + 31) / 32) * K.L + JAC_WARPS - 1) / JAC_WARPS);
   if (!tri.empty()) {
     // the most radii per thread that still gives two waves of CTAs
-    static int n_sm = 0;
-    if (n_sm == 0) {
-      int dev = 0;
-      if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
-        n_sm = 148;
-    }
+    const int n_sm = current_sm_count();
     auto ctas = [&](int R) {
       return (int64_t)(((int64_t)((K.L + R - 1) / R) * ((K.Me + 31) / 32) + JAC_WARPS - 1) / JAC_WARPS);
     };

@@ -14,6 +14,14 @@ int fail(int status, const std::string& msg);
 int cuda_fail(cudaError_t e, const char* what);
 void count_launch(int n = 1);
 
+// ---- per-device launch set-up (a process may drive several GPUs) ------------
+// SM count of the current device (148 when the query fails).
+int current_sm_count();
+// Raises fn's dynamic shared-memory limit to `bytes` on the current device,
+// once per (function, device): the attribute belongs to the device's context.
+// Returns PI_OK or the first attempt's error status.
+int ensure_smem_limit(const void* fn, int bytes, const char* what);
+
 #define PI_CUDA(call)                                        \
   do {                                                       \
     cudaError_t e_ = (call);                                 \
