@@ -358,7 +358,11 @@ def run_gb300(args):
             "dtype": "f32", "data": "synthetic (seeded)",
             "config": workload_config(meta, Q, world), "contraction_precision": precision,
             "vol_matrix_per_s": world * args.steps / (total_ms / 1e3),
-            "contraction": contraction, "clocks": clocks, "gpu_launches": launches, "roofline": roofline}
+            "contraction": contraction, "clocks": clocks, "gpu_launches": launches, "roofline": roofline,
+            "work_note": (f"value counts the workload's {evals_step:.4e} triangle x k pairs per step, all of them "
+                          f"produced in J; the form-factor kernel evaluates {evals_kernel:.4e} of them (one direction "
+                          f"of each antipodal pair, {n_eval_dirs} of {n_dirs}) and writes the rest as "
+                          "A(-k) = -conj A(k)")}
 
     if rank == 0 and not args.no_e2e:
         line["e2e"] = e2e_host(kg, objs, precision, args.steps, evals_step, world)
